@@ -1,0 +1,108 @@
+"""Seeded synthetic inputs for the benchmark and parity workloads.
+
+The workloads (sizes, seeds and distributions) are:
+
+* ``single_dipole`` -- one CCT bending-dipole layer: bending radius 0.95 m,
+  aperture radius 83 mm, 22.5 deg clockwise bend, tilt angles [30, 80, 90, 90]
+  deg, 128 turns x 360 segments (46 080 segments), 9000 A, placed after a
+  0.1 m drift along +x; 32 protons at 250 MeV with (x, xp) and (y, yp)
+  uniform inside a 3.5 mm x 7.5 mrad ellipse and delta uniform in +-1 %,
+  tracked 0.95 m x 22.5 deg (0.37306 m) at a 1 mm RK4 step (374 steps).
+* ``field_map`` -- 2**20 field points uniform in a 60 mm-radius tube around the
+  single-dipole design arc (uniform in arc length and in the disc).
+* ``gantry_section`` -- the HUST gantry second bending section with AG-CCT tilt
+  angles [90, 30, 90, 90], AG current -7000 A and 600 segments per turn
+  (597 600 segments, 16 CCT layers + 1 QS); 4096 protons at 215 MeV with
+  Gaussian sigma_x = 1 mm, sigma_xp = 2 mrad (same in y) and delta uniform in
+  +-2 %, RK4 step 1 mm over 3.5 m.
+* ``design_population`` -- 64 second-section designs with seeded tilt angles,
+  currents and winding counts (uneven segment totals), 512 protons each.
+
+Only numpy is used here; geometry is built by the package's beamline module.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+MM = 0.001
+
+SINGLE_DIPOLE = dict(drift=0.1, big_r=0.95, small_r=83 * MM, bending_angle=22.5, clockwise=True,
+                     tilt_angles=[30.0, 80.0, 90.0, 90.0], winding_number=128, current=9000.0,
+                     disperse_number_per_winding=360, kinetic_MeV=250.0, footstep=1 * MM)
+
+
+def single_dipole_track_length() -> float:
+    return SINGLE_DIPOLE["big_r"] * math.radians(SINGLE_DIPOLE["bending_angle"])
+
+
+def uniform_ellipse_phase_space(n: int, seed: int, x_max=3.5 * MM, xp_max=7.5 * MM, y_max=3.5 * MM,
+                                yp_max=7.5 * MM, delta_max=0.01) -> np.ndarray:
+    """(n, 6) phase-space tuples (x, xp, y, yp, z, delta): (x, xp) and (y, yp)
+    uniform inside the ellipses, z = 0, delta uniform in +-delta_max."""
+    rng = np.random.default_rng(seed)
+    out = np.zeros((n, 6))
+    for col, (a, b) in ((0, (x_max, xp_max)), (2, (y_max, yp_max))):
+        r = np.sqrt(rng.random(n))
+        t = rng.random(n) * 2 * math.pi
+        out[:, col] = a * r * np.cos(t)
+        out[:, col + 1] = b * r * np.sin(t)
+    out[:, 5] = rng.uniform(-delta_max, delta_max, n)
+    return out
+
+
+def gaussian_phase_space(n: int, seed: int, sx=1 * MM, sxp=2 * MM, sy=1 * MM, syp=2 * MM,
+                         delta_max=0.02) -> np.ndarray:
+    """(n, 6) Gaussian transverse phase space, delta uniform in +-delta_max."""
+    rng = np.random.default_rng(seed)
+    out = np.zeros((n, 6))
+    out[:, 0] = rng.normal(0.0, sx, n)
+    out[:, 1] = rng.normal(0.0, sxp, n)
+    out[:, 2] = rng.normal(0.0, sy, n)
+    out[:, 3] = rng.normal(0.0, syp, n)
+    out[:, 5] = rng.uniform(-delta_max, delta_max, n)
+    return out
+
+
+def field_map_points(n: int, seed: int = 1, tube_radius: float = 60 * MM) -> np.ndarray:
+    """(n, 3) points uniform in a tube around the single-dipole design arc.
+
+    The arc starts at (drift, 0, 0) heading +x and bends clockwise with radius R
+    about the centre (drift, -R, 0)."""
+    c = SINGLE_DIPOLE
+    R, d0 = c["big_r"], c["drift"]
+    L = single_dipole_track_length()
+    rng = np.random.default_rng(seed)
+    s = rng.random(n) * L
+    rho = tube_radius * np.sqrt(rng.random(n))
+    th = rng.random(n) * 2 * math.pi
+    phi = math.pi / 2 - s / R
+    radial = np.stack([np.cos(phi), np.sin(phi), np.zeros(n)], axis=1)
+    base = np.stack([d0 + R * np.cos(phi), -R + R * np.sin(phi), np.zeros(n)], axis=1)
+    return base + (rho * np.cos(th))[:, None] * radial + (rho * np.sin(th))[:, None] * np.array([0, 0, 1.0])
+
+
+GANTRY_SECTION = dict(agcct345_tilt_angles=[90.0, 30.0, 90.0, 90.0], agcct345_current=-7000.0,
+                      part_per_winding=600, kinetic_MeV=215.0, footstep=1 * MM, track_length=3.5)
+
+
+def design_population(n: int, seed: int = 3, part_per_winding: int = 360):
+    """Seeded second-section design parameters (keyword arguments of the
+    HUST_SC_GANTRY builder): 4 dipole + 4 AG tilt angles uniform in [20, 160]
+    deg, dipole and AG currents uniform in [-10000, 10000] A, dipole winding
+    count uniform in [64, 160] and AG part winding counts uniform in [21, 100]."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n):
+        t = rng.uniform(20.0, 160.0, 8)
+        cur = rng.uniform(-10000.0, 10000.0, 2)
+        wd = int(rng.integers(64, 161))
+        wa = [int(w) for w in rng.integers(21, 101, 3)]
+        out.append(dict(dicct345_tilt_angles=[float(x) for x in t[:4]],
+                        agcct345_tilt_angles=[float(x) for x in t[4:]],
+                        dicct345_current=float(cur[0]), agcct345_current=float(cur[1]),
+                        dicct345_winding_number=wd, agcct3_winding_number=wa[0],
+                        agcct4_winding_number=wa[1], agcct5_winding_number=wa[2],
+                        part_per_winding=part_per_winding))
+    return out

@@ -1,0 +1,126 @@
+/*
+ * cctgpu.h -- C ABI of the GB300 (sm_103a) Biot-Savart / RK4 tracking engine
+ * for CCT (canted-cosine-theta) magnet beamlines.
+ *
+ * Every entry point takes plain pointers and sizes, returns a cct_status, and
+ * records a message retrievable with cct_last_error().  Pointers named d_* are
+ * device pointers (any allocator: cudaMalloc, torch, ...); pointers named h_*
+ * are host pointers.  `stream` is a cudaStream_t passed as void* (NULL = the
+ * legacy default stream).  Calls are asynchronous on `stream` unless stated.
+ *
+ * Data layouts (all little-endian, C order):
+ *   segments   d_kls[n_seg*3], d_p0s[n_seg*3]  -- per straight current element,
+ *              kl = 1e-7 * I * (p[i+1]-p[i]) and p0 = (p[i+1]+p[i])/2 in the
+ *              GLOBAL frame, FP64, xyz interleaved: exactly the two flat arrays
+ *              of CCT.global_current_elements_and_elementary_current_positions
+ *              (cctpy final_code/packages/cct.py:434-457).  Several designs
+ *              are concatenated; d_seg_off[n_designs+1] (int64, device) gives
+ *              each design's first segment.
+ *   QS         d_qs[n_qs*16], FP64: origin, XI, YI, ZI, length, gradient,
+ *              second gradient, aperture radius -- QS.to_numpy_array
+ *              (cctpy final_code/packages/magnets.py:726-748).  Per design
+ *              ranges in d_qs_off[n_designs+1].
+ *   points     d_points[n*3] FP64 global xyz; fields d_B[n*3] FP64 tesla.
+ *   particles  d_particles[n_designs*n_particles*10] FP64 records
+ *              (px,py,pz,vx,vy,vz,relativistic mass,charge,speed,distance),
+ *              RunningParticle.to_numpy_array_data (cctpy particles.py:443-457).
+ */
+#ifndef CCTGPU_H
+#define CCTGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    CCT_OK = 0,
+    CCT_ERR_ARG = 1,         /* bad size, pointer or alignment (ValueError in Python) */
+    CCT_ERR_CUDA = 2,        /* a CUDA runtime call or launch failed */
+    CCT_ERR_TIMEOUT = 3,     /* a bounded device-side wait gave up */
+    CCT_ERR_NONFINITE = 4,   /* a particle state became NaN/Inf */
+    CCT_ERR_UNSUPPORTED = 5  /* device or configuration not supported */
+} cct_status;
+
+/* Library version (major*10000 + minor*100 + patch). */
+int cct_version(void);
+
+/* Copies the last error message of the calling thread into buf (NUL
+ * terminated, truncated to n bytes).  Returns the last status code. */
+int cct_last_error(char *buf, size_t n);
+
+/* Tile length (segments) of the FP32-compensated packed form. */
+int cct_f32c_tile(void);
+
+/* ---------------------------------------------------------------------------
+ * Field at points.
+ * Replaces the per-point CPU sum CCT.magnetic_field_at (cct.py:249-285) summed
+ * over a beamline (Beamline.magnetic_field_at, beamline.py:46-53) and the
+ * block-per-point CUDA kernels current_element_B / magnet_with_multi_qs
+ * (gpu_accelerator.py:363-383, :512-526).  B = sum over segments of
+ * kl x r / |r|^3 (r = point - p0) plus the analytic QS field of every QS.
+ * ------------------------------------------------------------------------- */
+
+/* Plain FP64 form (the drop-in). */
+int cct_field_f64(const double *d_kls, const double *d_p0s, int64_t n_seg,
+                  const double *d_qs, int32_t n_qs,
+                  const double *d_points, int64_t n_points, double *d_B,
+                  void *stream);
+
+/* FP32-compensated form: segments re-packed once into tiles of
+ * cct_f32c_tile() segments, each with an FP64 origin and FP32 offsets; the
+ * sum runs in FP32 with Kahan-compensated tile partials and FP64 cross-tile
+ * accumulation.  `packed` must be 256-byte aligned and hold
+ * cct_f32c_packed_bytes() bytes. */
+int64_t cct_f32c_packed_bytes(const int64_t *h_seg_off, int32_t n_designs);
+int cct_f32c_pack(const double *d_kls, const double *d_p0s,
+                  const int64_t *h_seg_off, int32_t n_designs,
+                  void *d_packed, int64_t packed_bytes, void *stream);
+int cct_field_f32c(const void *d_packed, int32_t design,
+                   const double *d_qs, int32_t n_qs,
+                   const double *d_points, int64_t n_points, double *d_B,
+                   void *stream);
+
+/* Host-buffer convenience form of cct_field_f64 / cct_field_f32c used as the
+ * end-to-end call: copies h_kls/h_p0s/h_points to the device, evaluates, and
+ * copies B back; synchronous.  precision: 0 = FP64, 1 = FP32-compensated.
+ * Allocates device memory internally. */
+int cct_field_host(const double *h_kls, const double *h_p0s, int64_t n_seg,
+                   const double *h_qs, int32_t n_qs,
+                   const double *h_points, int64_t n_points, double *h_B,
+                   int32_t precision);
+
+/* ---------------------------------------------------------------------------
+ * Batched RK4 tracking of n_particles protons through each of n_designs
+ * beamlines (particles of design d at d_particles + d*n_particles*10; updated
+ * in place).  Replaces ParticleRunner.run_only (particles.py:562-632, RK4 of
+ * base_utils.py:264-311) and the GPU tracking kernels
+ * track_multi_particle_beamline_for_magnet_with_multi_qs
+ * (gpu_accelerator.py:1044-1063, host wrapper :1912-2044).  Step semantics
+ * follow the CPU reference: dt = footstep/speed, t_end = distance/speed,
+ * steps = ceil(t_end/dt), dt := t_end/steps, Y' = [v, (e/m) v x B(p)],
+ * distance += `distance`.
+ *
+ * One cooperative persistent launch; CTAs meet at bounded grid barriers
+ * between RK4 stages.  Needs caller-provided device scratch of
+ * cct_track_scratch_bytes() bytes (256-byte aligned).  Returns
+ * CCT_ERR_TIMEOUT if a barrier wait gives up and CCT_ERR_NONFINITE if a
+ * particle state became non-finite (those particles are still written).
+ * Synchronous (reads the device status word before returning).
+ * precision: 0 = FP64 (d_kls/d_p0s used), 1 = FP32-compensated (d_packed
+ * used, built by cct_f32c_pack with the same design offsets).
+ * ------------------------------------------------------------------------- */
+int64_t cct_track_scratch_bytes(int32_t n_designs, int64_t n_particles);
+int cct_track(const double *d_kls, const double *d_p0s, const int64_t *d_seg_off,
+              const void *d_packed,
+              const double *d_qs, const int64_t *d_qs_off, int32_t n_designs,
+              double *d_particles, int64_t n_particles,
+              double distance, double footstep, int32_t precision,
+              void *d_scratch, int64_t scratch_bytes, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CCTGPU_H */
