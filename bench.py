@@ -1,0 +1,323 @@
+"""Benchmark: Biot-Savart Gpairs/s on the field-map workload, FP32-compensated vs FP64.
+
+Workload (one step): the field of the single CCT bending dipole (46 080 winding
+segments: R 0.95 m, r 83 mm, 22.5 deg, tilts [30, 80, 90, 90], 128 turns x 360,
+9000 A) at 2**20 seeded points uniform in a 60 mm tube around its design arc:
+2**20 x 46 080 = 4.832e10 pairs per step.  Synthetic inputs stand in for
+measured data (there is none in the reference for this path).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line.  `value` = FP32c Gpairs/s with inputs resident in HBM
+(device-timed; L2 flushed between steps); `e2e` = the same metric through the
+package's public call with pinned host points and a host result (copies inside
+the timed region); `fp64` = the plain FP64 drop-in on the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+N_POINTS = 1 << 20
+N_SEG = 46080
+PAIRS = N_POINTS * N_SEG
+FLOPS_PER_PAIR = 26
+METRIC = "Biot-Savart Gpairs/s & design-grads/s, 1 GB300: FP32+comp vs FP64 @1e-7 rel"
+WORKLOAD = "field_map: 2^20 points x 46080-segment single CCT dipole"
+
+
+def rank_info():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+# ---------------------------------------------------------------- clocks
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        rows = []
+        try:
+            for line in open(self.path):
+                f = [x.strip() for x in line.split(",")]
+                if len(f) >= 9 and f[1].replace(".", "").isdigit():
+                    rows.append(f)
+        except OSError:
+            pass
+        finally:
+            if self.path and os.path.exists(self.path):
+                os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no nvidia-smi samples"], "samples": 0}
+        sm = [float(r[1]) for r in rows]
+        mx = max(float(r[2]) for r in rows)
+        busy = [s for s in sm if s > 0.5 * mx] or sm
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(busy), "sm_max_mhz": mx, "reasons": reasons, "samples": len(rows),
+                "power_w_max": max(float(r[3]) for r in rows if r[3].replace(".", "").isdigit())}
+
+
+# ---------------------------------------------------------------- CPU oracle (reference arm / cpu_baseline)
+def oracle_field_sample(n_points: int, seed: int, processes: int):
+    """Time the CPU oracle (numpy restatement of cctpy's CCT.magnetic_field_at, over a spawn
+    process pool on all cores) on n_points points of the same workload.  Returns pairs/s."""
+    from oracle import cct_oracle as O
+    from cctpy_gb300 import workloads as W
+    c = W.SINGLE_DIPOLE
+    orb = O.Orbit((0.0, 0.0), (1.0, 0.0), c["drift"]).add_arc(c["big_r"], c["clockwise"], c["bending_angle"])
+    rec = O.cct_along(orb, c["drift"], c["big_r"], c["small_r"], c["bending_angle"], c["tilt_angles"],
+                      c["winding_number"], c["current"], (0.0, 0.0),
+                      (2 * math.pi * c["winding_number"], O.deg2rad(-c["bending_angle"])),
+                      c["disperse_number_per_winding"])
+    pts = W.field_map_points(n_points, seed=seed)
+    t0 = time.perf_counter()
+    O.field_many([rec], pts, processes=processes)
+    dt = time.perf_counter() - t0
+    return n_points * N_SEG / dt, dt
+
+
+def run_reference(args):
+    rank, world, _ = rank_info()
+    if rank != 0:
+        return
+    cores = os.cpu_count() or 1
+    n = args.ref_points
+    for _ in range(max(args.warmup, 0) and 1):
+        oracle_field_sample(max(cores * 4, 64), seed=100, processes=cores)
+    rates, times = [], []
+    for k in range(args.steps):
+        r, dt = oracle_field_sample(n, seed=200 + k, processes=cores)
+        rates.append(r)
+        times.append(dt)
+    value = (n * N_SEG * args.steps) / sum(times) / 1e9
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "Gpairs/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "n_points_per_step": n, "n_segments": N_SEG,
+                       "sample": f"{n} of the 2^20 field points per step"},
+            "cpu_baseline": {"value": value, "unit": "Gpairs/s", "cores": cores, "kind": "port",
+                             "sample": f"{n} points x {N_SEG} segments per step, {args.steps} steps"},
+            "e2e": {"value": value, "unit": "Gpairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------- GPU arm
+def run_ours(args):
+    import torch
+    rank, world, local = rank_info()
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    from cctpy_gb300 import _lib, engine, workloads as W
+    import ctypes
+
+    lib = _lib.load()
+    dev = torch.device("cuda", local)
+    _, cct = W.build_single_dipole()
+    ds = engine.design_of(cct)
+    assert ds.n_segments == N_SEG
+    packed = ds.packed()
+    pts_np = W.field_map_points(N_POINTS, seed=1 + rank)
+    pts = torch.from_numpy(pts_np).to(dev)
+    out = torch.empty_like(pts)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)   # > 129 MB L2
+    stream = torch.cuda.current_stream()
+    sptr = stream.cuda_stream
+
+    def f32c_step():
+        rc = lib.cct_field_f32c(packed.data_ptr(), 0, None, 0, pts.data_ptr(), N_POINTS, out.data_ptr(), sptr)
+        if rc:
+            _lib.check(rc, "cct_field_f32c")
+
+    def f64_step():
+        rc = lib.cct_field_f64(ds.kls.data_ptr(), ds.p0s.data_ptr(), N_SEG, None, 0, pts.data_ptr(), N_POINTS,
+                               out.data_ptr(), sptr)
+        if rc:
+            _lib.check(rc, "cct_field_f64")
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    # ---- accuracy of the timed kernel on the full workload (FP32c vs FP64, same points)
+    f64_step()
+    torch.cuda.synchronize()
+    b64 = out.clone()
+    f32c_step()
+    torch.cuda.synchronize()
+    rel = (torch.linalg.norm(out - b64, dim=1) / torch.linalg.norm(b64, dim=1))
+    acc = {"max_rel_f32c_vs_f64": float(rel.max()), "rms_rel_f32c_vs_f64": float(torch.sqrt((rel ** 2).mean()))}
+
+    # ---- FP32c, device-resident, K timed steps with per-step kernel events
+    for _ in range(args.warmup):
+        flush.zero_()
+        f32c_step()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    barrier()
+    with ClockSampler(local) as clk:
+        t0 = torch.cuda.Event(enable_timing=True)
+        t1 = torch.cuda.Event(enable_timing=True)
+        t0.record()
+        for k in range(args.steps):
+            flush.zero_()
+            ev[k][0].record()
+            f32c_step()
+            ev[k][1].record()
+        t1.record()
+        barrier()
+    total_ms = t0.elapsed_time(t1)
+    kern_ms = [a.elapsed_time(b) for a, b in ev]
+    clocks = clk.summary()
+    if dist is not None:
+        t = torch.tensor([total_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t)
+    value = world * PAIRS * args.steps / (total_ms * 1e-3) / 1e9
+    kernel_ms = statistics.mean(kern_ms)
+
+    # ---- roofline: FP32 FMA pipe, measured live
+    peak = ctypes.c_double()
+    _lib.check(lib.cct_probe_fma_peak(0, ctypes.byref(peak)), "cct_probe_fma_peak")
+    peak32 = peak.value / 1e12
+    _lib.check(lib.cct_probe_fma_peak(1, ctypes.byref(peak)), "cct_probe_fma_peak")
+    peak64 = peak.value / 1e12
+    achieved = FLOPS_PER_PAIR * PAIRS / (kernel_ms * 1e-3) / 1e12
+
+    # ---- FP64 drop-in on the same workload
+    f64_steps = max(1, args.fp64_steps)
+    f64_step()
+    barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(f64_steps):
+        flush.zero_()
+        f64_step()
+    e1.record()
+    barrier()
+    f64_ms = e0.elapsed_time(e1) / f64_steps
+    f64_value = PAIRS / (f64_ms * 1e-3) / 1e9
+    f64_achieved = FLOPS_PER_PAIR * PAIRS / (f64_ms * 1e-3) / 1e12
+
+    # ---- end to end through the public call: pinned host points in, host field out
+    h_pts = torch.from_numpy(pts_np).pin_memory()
+    h_out = torch.empty_like(h_pts).pin_memory()
+    for _ in range(2):
+        engine.field_at_points(ds, h_pts, "f32c", out_host=h_out)
+    barrier()
+    w0 = time.perf_counter()
+    for _ in range(args.steps):
+        engine.field_at_points(ds, h_pts, "f32c", out_host=h_out)
+    barrier()
+    e2e_s = time.perf_counter() - w0
+    if dist is not None:
+        t = torch.tensor([e2e_s], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t)
+    e2e = world * PAIRS * args.steps / e2e_s / 1e9
+
+    line = None
+    if rank == 0:
+        cpu = None
+        if world == 1 and not args.no_cpu_baseline:
+            cores = os.cpu_count() or 1
+            n = args.cpu_points
+            rate, dt = oracle_field_sample(n, seed=300, processes=cores)
+            cpu = {"value": rate / 1e9, "unit": "Gpairs/s", "cores": cores, "kind": "port",
+                   "sample": f"{n} of the 2^20 points x {N_SEG} segments ({dt:.1f} s, numpy oracle over a "
+                             f"{cores}-process spawn pool)"}
+        line = {
+            "metric": METRIC, "value": value, "unit": "Gpairs/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32+comp (f64 origins/accumulation)",
+            "data": "synthetic (seeded points in a 60 mm tube around the dipole arc)",
+            "config": {"workload": WORKLOAD, "n_points": N_POINTS, "n_segments": N_SEG, "pairs_per_step": PAIRS,
+                       "precision": "f32c", "l2": "256 MiB buffer written between timed steps",
+                       "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
+            "e2e": {"value": e2e, "unit": "Gpairs/s", "h2d_bytes_per_step": N_POINTS * 24,
+                    "d2h_bytes_per_step": N_POINTS * 24,
+                    "call": "engine.field_at_points(design, pinned host points, 'f32c', out_host=pinned)"},
+            "roofline": {"bound": "fp32-pipe", "achieved": achieved, "peak": peak32, "unit": "TFLOP/s",
+                         "frac": achieved / peak32, "traffic": args.traffic,
+                         "peak_source": "measured in this run: FP32 FFMA-chain probe (cct_probe_fma_peak)",
+                         "flops_per_pair": FLOPS_PER_PAIR, "kernel": "field_f32c_kernel",
+                         "kernel_ms": kernel_ms},
+            "fp64": {"value": f64_value, "unit": "Gpairs/s", "ms_per_step": f64_ms, "steps": f64_steps,
+                     "roofline": {"bound": "fp64-pipe", "achieved": f64_achieved, "peak": peak64,
+                                  "unit": "TFLOP/s", "frac": f64_achieved / peak64,
+                                  "peak_source": "measured in this run: FP64 DFMA-chain probe"},
+                     "speedup_f32c_vs_f64": value / f64_value},
+            "accuracy": acc,
+            "gpu_launches": args.steps,
+            "clocks": clocks,
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--fp64-steps", type=int, default=2)
+    ap.add_argument("--cpu-points", type=int, default=16384)
+    ap.add_argument("--ref-points", type=int, default=4096)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--traffic", type=float, default=None,
+                    help="DRAM bytes per launch of the timed kernel from an ncu capture")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "ours":
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,316 @@
+// Biot-Savart field of CCT winding segments (+ analytic QS magnets) at field points.
+//
+//   B(p) = sum_i kl_i x r_i / |r_i|^3,  r_i = p - p0_i,  kl_i = 1e-7 I (w[i+1]-w[i]),
+//   p0_i = (w[i+1]+w[i])/2            -- cctpy final_code/packages/cct.py:157-164, :249-285
+//
+// Two forms:
+//  * field_f64_kernel   plain FP64, one thread per field point (x2), segment tiles staged in
+//                       shared memory by the CTA; the drop-in for CCT.magnetic_field_at.
+//  * field_f32c_kernel  FP32 arithmetic on per-tile local offsets: each tile of 128 segments
+//                       carries an FP64 origin, the point-minus-origin subtraction is FP64,
+//                       the 128 pair terms run in FP32 (rsqrt on the MUFU pipe) summed in
+//                       sub-blocks of 32 with a Kahan-compensated tile partial, and tile
+//                       partials accumulate in FP64.  Tiles are streamed into shared memory
+//                       by the TMA bulk-copy engine through a 4-deep mbarrier ring.
+#include <cstdarg>
+#include <cstdio>
+#include <vector>
+
+#include "cctgpu_internal.cuh"
+#include "qs.cuh"
+#include "tile.cuh"
+
+namespace cctgpu {
+
+// ===================================================================== FP64
+constexpr int kF64Block = 256;
+constexpr int kF64Ppt = 2;
+
+__global__ void __launch_bounds__(kF64Block) field_f64_kernel(const double *__restrict__ kls,
+                                                              const double *__restrict__ p0s, int64_t n_seg,
+                                                              const double *__restrict__ qs, int n_qs,
+                                                              const double *__restrict__ pts, int64_t n,
+                                                              double *__restrict__ B) {
+    __shared__ double sk[3][kF64Block];
+    __shared__ double sp[3][kF64Block];
+    const int tid = threadIdx.x;
+    const int64_t base = (int64_t)blockIdx.x * kF64Block * kF64Ppt;
+
+    double px[kF64Ppt], py[kF64Ppt], pz[kF64Ppt], bx[kF64Ppt], by[kF64Ppt], bz[kF64Ppt];
+#pragma unroll
+    for (int i = 0; i < kF64Ppt; ++i) {
+        int64_t idx = base + tid + (int64_t)i * kF64Block;
+        if (idx >= n) idx = n - 1;
+        px[i] = pts[3 * idx];
+        py[i] = pts[3 * idx + 1];
+        pz[i] = pts[3 * idx + 2];
+        bx[i] = by[i] = bz[i] = 0.0;
+    }
+
+    for (int64_t t0 = 0; t0 < n_seg; t0 += kF64Block) {
+        const int64_t s = t0 + tid;
+        __syncthreads();
+        if (s < n_seg) {
+            sk[0][tid] = kls[3 * s];
+            sk[1][tid] = kls[3 * s + 1];
+            sk[2][tid] = kls[3 * s + 2];
+            sp[0][tid] = p0s[3 * s];
+            sp[1][tid] = p0s[3 * s + 1];
+            sp[2][tid] = p0s[3 * s + 2];
+        }
+        __syncthreads();
+        const int cnt = (int)min((int64_t)kF64Block, n_seg - t0);
+        double tx[kF64Ppt], ty[kF64Ppt], tz[kF64Ppt];
+#pragma unroll
+        for (int i = 0; i < kF64Ppt; ++i) tx[i] = ty[i] = tz[i] = 0.0;
+#pragma unroll 2
+        for (int j = 0; j < cnt; ++j) {
+            const double kx = sk[0][j], ky = sk[1][j], kz = sk[2][j];
+            const double qx = sp[0][j], qy = sp[1][j], qz = sp[2][j];
+#pragma unroll
+            for (int i = 0; i < kF64Ppt; ++i) {
+                const double rx = px[i] - qx, ry = py[i] - qy, rz = pz[i] - qz;
+                const double inv = rsqrt(rx * rx + ry * ry + rz * rz);
+                const double inv3 = inv * inv * inv;
+                tx[i] += (ky * rz - kz * ry) * inv3;
+                ty[i] += (kz * rx - kx * rz) * inv3;
+                tz[i] += (kx * ry - ky * rx) * inv3;
+            }
+        }
+#pragma unroll
+        for (int i = 0; i < kF64Ppt; ++i) {
+            bx[i] += tx[i];
+            by[i] += ty[i];
+            bz[i] += tz[i];
+        }
+    }
+
+#pragma unroll
+    for (int i = 0; i < kF64Ppt; ++i) {
+        const int64_t idx = base + tid + (int64_t)i * kF64Block;
+        if (idx >= n) continue;
+        for (int q = 0; q < n_qs; ++q) qs_field_add(qs + kQsRecord * q, px[i], py[i], pz[i], bx[i], by[i], bz[i]);
+        B[3 * idx] = bx[i];
+        B[3 * idx + 1] = by[i];
+        B[3 * idx + 2] = bz[i];
+    }
+}
+
+int launch_field_f64(const double *kls, const double *p0s, int64_t n_seg, const double *qs, int n_qs,
+                     const double *pts, int64_t n, double *B, cudaStream_t st) {
+    if (n == 0) return CCT_OK;
+    const int64_t per = (int64_t)kF64Block * kF64Ppt;
+    const int64_t grid = (n + per - 1) / per;
+    if (grid > 0x7fffffff) return set_error(CCT_ERR_ARG, "too many field points (%lld)", (long long)n);
+    field_f64_kernel<<<(unsigned)grid, kF64Block, 0, st>>>(kls, p0s, n_seg, qs, n_qs, pts, n, B);
+    CCT_TRY_CUDA(cudaGetLastError());
+    return CCT_OK;
+}
+
+// ===================================================================== FP32c pack
+// Tile layout (kTileBytes = 3104, 16-byte multiple):
+//   double origin[3]; double count;          (32 B)
+//   float kx[128], ky[128], kz[128];         kl components
+//   float px[128], py[128], pz[128];         p0 - origin
+__global__ void __launch_bounds__(kTile) pack_f32c_kernel(const double *__restrict__ kls,
+                                                          const double *__restrict__ p0s,
+                                                          unsigned char *__restrict__ packed) {
+    const int64_t n_designs = reinterpret_cast<const int64_t *>(packed)[1];
+    const int64_t *tile_off = reinterpret_cast<const int64_t *>(packed + kPackedHeaderBytes);
+    const int64_t *seg_off = tile_off + (n_designs + 1);
+    unsigned char *tiles = packed + kPackedHeaderBytes + packed_index_bytes((int)n_designs);
+    const int64_t t = blockIdx.x;
+    // design holding tile t: last d with tile_off[d] <= t
+    int64_t lo = 0, hi = n_designs - 1;
+    while (lo < hi) {
+        const int64_t mid = (lo + hi + 1) / 2;
+        if (tile_off[mid] <= t) lo = mid; else hi = mid - 1;
+    }
+    const int64_t d = lo;
+    const int64_t s0 = seg_off[d] + (t - tile_off[d]) * kTile;
+    const int cnt = (int)min((int64_t)kTile, seg_off[d + 1] - s0);
+    const int i = threadIdx.x;
+
+    __shared__ double red[3][kTile];
+    double k[3] = {0.0, 0.0, 0.0}, p[3] = {0.0, 0.0, 0.0};
+    if (i < cnt) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            k[c] = kls[3 * (s0 + i) + c];
+            p[c] = p0s[3 * (s0 + i) + c];
+        }
+    }
+#pragma unroll
+    for (int c = 0; c < 3; ++c) red[c][i] = p[c];
+    __syncthreads();
+    for (int w = kTile / 2; w > 0; w >>= 1) {   // fixed-order tree: deterministic origin
+        if (i < w) {
+#pragma unroll
+            for (int c = 0; c < 3; ++c) red[c][i] += red[c][i + w];
+        }
+        __syncthreads();
+    }
+    double o[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) o[c] = cnt > 0 ? red[c][0] / cnt : 0.0;
+
+    unsigned char *tile = tiles + t * (int64_t)kTileBytes;
+    double *hdr = reinterpret_cast<double *>(tile);
+    float *f = reinterpret_cast<float *>(tile + kTileHeaderBytes);
+    if (i == 0) {
+        hdr[0] = o[0];
+        hdr[1] = o[1];
+        hdr[2] = o[2];
+        hdr[3] = (double)cnt;
+    }
+    if (i < cnt) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            f[c * kTile + i] = (float)k[c];
+            f[(3 + c) * kTile + i] = (float)(p[c] - o[c]);
+        }
+    } else {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            f[c * kTile + i] = 0.0f;
+            f[(3 + c) * kTile + i] = kPadOffset;
+        }
+    }
+}
+
+int launch_pack_f32c(const double *kls, const double *p0s, const int64_t *h_seg_off, int n_designs,
+                     void *packed, int64_t packed_bytes, cudaStream_t st) {
+    std::vector<int64_t> hdr(kPackedHeaderBytes / 8 + 2 * (n_designs + 1), 0);
+    int64_t *tile_off = hdr.data() + kPackedHeaderBytes / 8;
+    int64_t *seg_off = tile_off + (n_designs + 1);
+    tile_off[0] = 0;
+    for (int d = 0; d < n_designs; ++d) {
+        const int64_t ns = h_seg_off[d + 1] - h_seg_off[d];
+        tile_off[d + 1] = tile_off[d] + (ns + kTile - 1) / kTile;
+    }
+    for (int d = 0; d <= n_designs; ++d) seg_off[d] = h_seg_off[d];
+    hdr[0] = kPackedMagic;
+    hdr[1] = n_designs;
+    hdr[2] = tile_off[n_designs];
+    const int64_t need = kPackedHeaderBytes + packed_index_bytes(n_designs) + tile_off[n_designs] * kTileBytes;
+    if (packed_bytes < need)
+        return set_error(CCT_ERR_ARG, "packed buffer holds %lld bytes, needs %lld", (long long)packed_bytes,
+                         (long long)need);
+    CCT_TRY_CUDA(cudaMemcpyAsync(packed, hdr.data(), hdr.size() * 8, cudaMemcpyHostToDevice, st));
+    if (tile_off[n_designs] > 0) {
+        pack_f32c_kernel<<<(unsigned)tile_off[n_designs], kTile, 0, st>>>(kls, p0s,
+                                                                         static_cast<unsigned char *>(packed));
+        CCT_TRY_CUDA(cudaGetLastError());
+    }
+    // the header copy reads a host vector that goes out of scope here
+    CCT_TRY_CUDA(cudaStreamSynchronize(st));
+    return CCT_OK;
+}
+
+// ===================================================================== FP32c field
+constexpr int kF32Block = 256;
+constexpr int kF32Ppt = 2;
+constexpr int kStages = 4;
+constexpr uint32_t kWaitPolls = 1u << 22;
+
+__device__ int g_field_status;   // last non-OK status seen by a field kernel (sticky)
+
+__global__ void __launch_bounds__(kF32Block, 2) field_f32c_kernel(const unsigned char *__restrict__ packed,
+                                                                  int design, const double *__restrict__ qs,
+                                                                  int n_qs, const double *__restrict__ pts,
+                                                                  int64_t n, double *__restrict__ B) {
+    __shared__ __align__(128) unsigned char buf[kStages][kTileBytes];
+    __shared__ __align__(8) uint64_t full[kStages];
+    const int tid = threadIdx.x;
+    const int64_t magic = reinterpret_cast<const int64_t *>(packed)[0];
+    const int64_t n_designs = reinterpret_cast<const int64_t *>(packed)[1];
+    const int64_t base = (int64_t)blockIdx.x * kF32Block * kF32Ppt;
+    if (magic != kPackedMagic || design >= n_designs) {   // not a packed set, or no such design
+        if (tid == 0 && blockIdx.x == 0) atomicExch(&g_field_status, (int)CCT_ERR_ARG);
+        for (int i = 0; i < kF32Ppt; ++i) {
+            const int64_t idx = base + tid + (int64_t)i * kF32Block;
+            if (idx < n) B[3 * idx] = B[3 * idx + 1] = B[3 * idx + 2] = __longlong_as_double(0x7ff8000000000000LL);
+        }
+        return;
+    }
+    const int64_t *tile_off = reinterpret_cast<const int64_t *>(packed + kPackedHeaderBytes);
+    const unsigned char *tiles = packed + kPackedHeaderBytes + packed_index_bytes((int)n_designs) +
+                                 tile_off[design] * (int64_t)kTileBytes;
+    const int64_t nt = tile_off[design + 1] - tile_off[design];
+
+    if (tid == 0) {
+        for (int s = 0; s < kStages; ++s) cctdev::mbar_init(&full[s], 1);
+        cctdev::mbar_fence_init();
+    }
+    __syncthreads();
+    if (tid == 0) {
+        for (int s = 0; s < kStages && s < nt; ++s) {
+            cctdev::mbar_arrive_expect_tx(&full[s], kTileBytes);
+            cctdev::bulk_g2s(buf[s], tiles + (int64_t)s * kTileBytes, kTileBytes, &full[s]);
+        }
+    }
+
+    double px[kF32Ppt], py[kF32Ppt], pz[kF32Ppt], bx[kF32Ppt], by[kF32Ppt], bz[kF32Ppt];
+#pragma unroll
+    for (int i = 0; i < kF32Ppt; ++i) {
+        int64_t idx = base + tid + (int64_t)i * kF32Block;
+        if (idx >= n) idx = n - 1;
+        px[i] = pts[3 * idx];
+        py[i] = pts[3 * idx + 1];
+        pz[i] = pts[3 * idx + 2];
+        bx[i] = by[i] = bz[i] = 0.0;
+    }
+
+    bool failed = false;
+    for (int64_t t = 0; t < nt; ++t) {
+        const int s = (int)(t % kStages);
+        const bool ok = cctdev::mbar_wait_bounded(&full[s], (uint32_t)((t / kStages) & 1), kWaitPolls);
+        // also orders: every thread has finished tile t-1 before its buffer is refilled
+        if (__syncthreads_or(!ok)) {
+            failed = true;
+            break;
+        }
+        if (tid == 0 && t >= 1 && t - 1 + kStages < nt) {
+            const int sp = (int)((t - 1) % kStages);
+            cctdev::fence_proxy_async();
+            cctdev::mbar_arrive_expect_tx(&full[sp], kTileBytes);
+            cctdev::bulk_g2s(buf[sp], tiles + (t - 1 + kStages) * (int64_t)kTileBytes, kTileBytes, &full[sp]);
+        }
+        tile_f32c<kF32Ppt>(buf[s], px, py, pz, bx, by, bz);
+    }
+    if (failed) {
+        // let copies still in flight land before the CTA's shared memory is released
+        if (tid == 0) {
+            for (int s = 0; s < kStages; ++s) (void)cctdev::mbar_wait_bounded(&full[s], 0, 1024);
+            atomicExch(&g_field_status, (int)CCT_ERR_TIMEOUT);
+        }
+    }
+
+#pragma unroll
+    for (int i = 0; i < kF32Ppt; ++i) {
+        const int64_t idx = base + tid + (int64_t)i * kF32Block;
+        if (idx >= n) continue;
+        if (failed) {
+            B[3 * idx] = B[3 * idx + 1] = B[3 * idx + 2] = __longlong_as_double(0x7ff8000000000000LL);
+            continue;
+        }
+        for (int q = 0; q < n_qs; ++q) qs_field_add(qs + kQsRecord * q, px[i], py[i], pz[i], bx[i], by[i], bz[i]);
+        B[3 * idx] = bx[i];
+        B[3 * idx + 1] = by[i];
+        B[3 * idx + 2] = bz[i];
+    }
+}
+
+int launch_field_f32c(const void *packed, int design, const double *qs, int n_qs, const double *pts, int64_t n,
+                      double *B, cudaStream_t st) {
+    if (n == 0) return CCT_OK;
+    const int64_t per = (int64_t)kF32Block * kF32Ppt;
+    const int64_t grid = (n + per - 1) / per;
+    if (grid > 0x7fffffff) return set_error(CCT_ERR_ARG, "too many field points (%lld)", (long long)n);
+    field_f32c_kernel<<<(unsigned)grid, kF32Block, 0, st>>>(static_cast<const unsigned char *>(packed), design, qs,
+                                                            n_qs, pts, n, B);
+    CCT_TRY_CUDA(cudaGetLastError());
+    return CCT_OK;
+}
+
+}  // namespace cctgpu

@@ -1,0 +1,248 @@
+"""Device-resident design sets and the calls into libcctgpu.
+
+A *design* is one beamline (or magnet) reduced to what the kernels read: its
+CCT current elements in the global frame (FP64, concatenated over layers) and
+its QS records.  A *design set* concatenates several designs with CSR offsets,
+so that one tracking launch covers a whole optimisation population.  Segment
+sets stay in HBM between calls (cached on the Python object); the FP32c packed
+form is built on first use.  Torch provides device memory and the stream.
+"""
+from __future__ import annotations
+
+import ctypes
+from typing import List, Sequence
+
+import numpy as np
+import torch
+
+from . import _lib
+
+_F32C_CACHE_ATTR = "_cctgpu_design"
+
+
+def _device() -> torch.device:
+    if not torch.cuda.is_available():
+        raise RuntimeError("cctpy_gb300 needs a CUDA device (GB300, sm_103a); none is visible")
+    return torch.device("cuda", torch.cuda.current_device())
+
+
+def _ptr(t) -> int:
+    return 0 if t is None or t.numel() == 0 else t.data_ptr()
+
+
+def _stream() -> int:
+    return torch.cuda.current_stream().cuda_stream
+
+
+def _classify(m):
+    """'cct' / 'qs' for magnets the kernels evaluate (this package's classes or any object
+    with cctpy's CCT / QS attributes); raises ValueError otherwise, as cctpy's GPU path does
+    (gpu_accelerator.py:1969-1970)."""
+    if hasattr(m, "winding_number") and hasattr(m, "tilt_angles") and hasattr(m, "local_coordinate_system"):
+        return "cct"
+    if hasattr(m, "second_gradient") and hasattr(m, "aperture_radius") and hasattr(m, "local_coordinate_system"):
+        return "qs"
+    raise ValueError(f"magnet {m} cannot be evaluated on the GPU (only CCT and QS are supported)")
+
+
+def magnet_list(obj) -> List:
+    """Flatten a Beamline / CombinedMagnet / magnet (ours or cctpy's) into CCT/QS magnets."""
+    if hasattr(obj, "magnets_for_gpu"):
+        return obj.magnets_for_gpu()
+    if hasattr(obj, "magnets"):               # cctpy Beamline
+        out = []
+        for m in obj.magnets:
+            out.extend(magnet_list(m))
+        return out
+    if hasattr(obj, "get_magnets"):           # cctpy CombinedMagnet
+        out = []
+        for m in obj.get_magnets():
+            out.extend(magnet_list(m))
+        return out
+    return [obj]
+
+
+def cct_global_segments(m):
+    """(kl, p0) global (N, 3) FP64 of a CCT (ours: vectorised; cctpy's: its own export)."""
+    if hasattr(m, "global_segments"):
+        return m.global_segments()
+    kl, p0 = m.global_current_elements_and_elementary_current_positions(np.float64)
+    return kl.reshape(-1, 3), p0.reshape(-1, 3)
+
+
+def qs_record(m) -> np.ndarray:
+    return np.asarray(m.to_numpy_array(np.float64), dtype=np.float64)
+
+
+def host_design(magnets: Sequence) -> tuple:
+    """(kls (N,3), p0s (N,3), qs (M,16)) of one design.  A CCT with |current| <= 1e-6
+    contributes nothing (cct.py:254-255)."""
+    kls, p0s, qss = [], [], []
+    for m in magnets:
+        kind = _classify(m)
+        if kind == "cct":
+            if abs(float(m.current)) <= 1e-6:
+                continue
+            kl, p0 = cct_global_segments(m)
+            kls.append(kl)
+            p0s.append(p0)
+        else:
+            qss.append(qs_record(m))
+    kl = np.concatenate(kls) if kls else np.zeros((0, 3))
+    p0 = np.concatenate(p0s) if p0s else np.zeros((0, 3))
+    qs = np.stack(qss) if qss else np.zeros((0, 16))
+    return np.ascontiguousarray(kl), np.ascontiguousarray(p0), np.ascontiguousarray(qs)
+
+
+class DesignSet:
+    """Several designs resident in HBM: segments (FP64), QS records, CSR offsets."""
+
+    def __init__(self, designs: Sequence[tuple]):
+        dev = _device()
+        self.n_designs = len(designs)
+        if self.n_designs == 0:
+            raise ValueError("empty design set")
+        seg_off = np.zeros(self.n_designs + 1, dtype=np.int64)
+        qs_off = np.zeros(self.n_designs + 1, dtype=np.int64)
+        for i, (kl, _, qs) in enumerate(designs):
+            seg_off[i + 1] = seg_off[i] + kl.shape[0]
+            qs_off[i + 1] = qs_off[i] + qs.shape[0]
+        self.h_seg_off = seg_off
+        self.h_qs_off = qs_off
+        cat = lambda k, w: np.concatenate([d[k] for d in designs]) if designs else np.zeros((0, w))
+        self.kls = torch.from_numpy(cat(0, 3)).to(dev)
+        self.p0s = torch.from_numpy(cat(1, 3)).to(dev)
+        self.qs = torch.from_numpy(cat(2, 16)).to(dev)
+        self.seg_off = torch.from_numpy(seg_off).to(dev)
+        self.qs_off = torch.from_numpy(qs_off).to(dev)
+        self._packed = None
+
+    @property
+    def n_segments(self) -> int:
+        return int(self.h_seg_off[-1])
+
+    def segments_of(self, d: int) -> int:
+        return int(self.h_seg_off[d + 1] - self.h_seg_off[d])
+
+    def packed(self) -> torch.Tensor:
+        """FP32c packed tiles (built once, on the current stream)."""
+        if self._packed is None:
+            lib = _lib.load()
+            off = self.h_seg_off.ctypes.data_as(ctypes.c_void_p)
+            nbytes = lib.cct_f32c_packed_bytes(off, self.n_designs)
+            _lib.check(0 if nbytes >= 0 else _lib.CCT_ERR_ARG, "cct_f32c_packed_bytes")
+            buf = torch.empty(int(nbytes) + 256, dtype=torch.uint8, device=self.kls.device)
+            shift = (-buf.data_ptr()) % 256
+            view = buf[shift:shift + int(nbytes)]
+            _lib.check(lib.cct_f32c_pack(_ptr(self.kls), _ptr(self.p0s), off, self.n_designs, view.data_ptr(),
+                                         int(nbytes), _stream()), "cct_f32c_pack")
+            self._packed_buf = buf
+            self._packed = view
+        return self._packed
+
+
+def design_of(obj) -> DesignSet:
+    """Single-design set of a magnet / beamline, cached on the object."""
+    ds = getattr(obj, _F32C_CACHE_ATTR, None)
+    if ds is None:
+        ds = DesignSet([host_design(magnet_list(obj))])
+        try:
+            setattr(obj, _F32C_CACHE_ATTR, ds)
+        except AttributeError:
+            pass
+    return ds
+
+
+def design_set_of(objs: Sequence) -> DesignSet:
+    return DesignSet([host_design(magnet_list(o)) for o in objs])
+
+
+def field_at_points(ds: DesignSet, points, precision: str = "f64", design: int = 0, out_host=None):
+    """Field of design `design` at (n, 3) points.
+
+    points: numpy array (-> numpy result), torch CUDA tensor (-> CUDA tensor, no copies) or
+    torch CPU tensor (-> CPU tensor; pinned memory gives asynchronous copies; `out_host`,
+    a CPU float64 tensor of the same shape, receives the result without an allocation)."""
+    lib = _lib.load()
+    dev = ds.kls.device
+    if not 0 <= design < ds.n_designs:
+        raise ValueError(f"design {design} not in a set of {ds.n_designs}")
+    as_numpy = not isinstance(points, torch.Tensor)
+    host_tensor = (not as_numpy) and not points.is_cuda
+    if as_numpy:
+        pts = torch.as_tensor(np.ascontiguousarray(points, dtype=np.float64), device=dev)
+    elif host_tensor:
+        pts = points.to(device=dev, dtype=torch.float64, non_blocking=True).contiguous()
+    else:
+        pts = points.to(dtype=torch.float64).contiguous()
+    if pts.ndim != 2 or pts.shape[1] != 3:
+        raise ValueError(f"points must have shape (n, 3), not {tuple(pts.shape)}")
+    out = torch.empty_like(pts)
+    a, b = int(ds.h_seg_off[design]), int(ds.h_seg_off[design + 1])
+    qa, qb = int(ds.h_qs_off[design]), int(ds.h_qs_off[design + 1])
+    qs = ds.qs[qa:qb]
+    if precision == "f64":
+        kls, p0s = ds.kls[a:b], ds.p0s[a:b]
+        rc = lib.cct_field_f64(_ptr(kls), _ptr(p0s), b - a, _ptr(qs), qb - qa, _ptr(pts), pts.shape[0], _ptr(out),
+                               _stream())
+        _lib.check(rc, "cct_field_f64")
+    elif precision == "f32c":
+        rc = lib.cct_field_f32c(ds.packed().data_ptr(), design, _ptr(qs), qb - qa, _ptr(pts), pts.shape[0],
+                                _ptr(out), _stream())
+        _lib.check(rc, "cct_field_f32c")
+    else:
+        raise ValueError(f"precision must be 'f64' or 'f32c', not {precision!r}")
+    if as_numpy:
+        return out.cpu().numpy()
+    if host_tensor:
+        res = out_host if out_host is not None else torch.empty(out.shape, dtype=torch.float64,
+                                                                 pin_memory=points.is_pinned())
+        res.copy_(out, non_blocking=res.is_pinned())
+        torch.cuda.current_stream().synchronize()
+        return res
+    return out
+
+
+_scratch_cache = {}
+
+
+def scratch(nbytes: int, dev) -> torch.Tensor:
+    key = (dev.index,)
+    buf = _scratch_cache.get(key)
+    if buf is None or buf.numel() < nbytes + 256:
+        buf = torch.empty(int(nbytes) + 256, dtype=torch.uint8, device=dev)
+        _scratch_cache[key] = buf
+    shift = (-buf.data_ptr()) % 256
+    return buf[shift:shift + int(nbytes)]
+
+
+def track(ds: DesignSet, particles, distance: float, footstep: float, precision: str = "f64"):
+    """RK4-track particle records through every design of `ds`.
+
+    particles: (n_designs, n_p, 10) or (n_p, 10) (broadcast to every design) FP64 records,
+    numpy or torch CUDA.  Returns (n_designs, n_p, 10) in the same kind."""
+    lib = _lib.load()
+    dev = ds.kls.device
+    as_numpy = not isinstance(particles, torch.Tensor)
+    p = torch.as_tensor(np.asarray(particles, dtype=np.float64) if as_numpy else particles, dtype=torch.float64,
+                        device=dev)
+    if p.ndim == 2:
+        p = p.unsqueeze(0).expand(ds.n_designs, -1, -1)
+    if p.ndim != 3 or p.shape[0] != ds.n_designs or p.shape[2] != 10:
+        raise ValueError(f"particles must be (n_designs, n, 10) or (n, 10), not {tuple(p.shape)}")
+    p = p.contiguous().clone()
+    n_p = p.shape[1]
+    if n_p == 0:
+        return p.cpu().numpy() if as_numpy else p
+    prec = {"f64": 0, "f32c": 1}.get(precision)
+    if prec is None:
+        raise ValueError(f"precision must be 'f64' or 'f32c', not {precision!r}")
+    packed = ds.packed() if prec == 1 else None
+    nbytes = lib.cct_track_scratch_bytes(ds.n_designs, n_p)
+    _lib.check(0 if nbytes >= 0 else _lib.CCT_ERR_ARG, "cct_track_scratch_bytes")
+    sc = scratch(nbytes, dev)
+    rc = lib.cct_track(_ptr(ds.kls), _ptr(ds.p0s), _ptr(ds.seg_off), 0 if packed is None else packed.data_ptr(),
+                       _ptr(ds.qs), _ptr(ds.qs_off), ds.n_designs, _ptr(p), n_p, float(distance), float(footstep),
+                       prec, sc.data_ptr(), int(nbytes), _stream())
+    _lib.check(rc, "cct_track")
+    return p.cpu().numpy() if as_numpy else p

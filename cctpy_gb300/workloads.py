@@ -106,3 +106,51 @@ def design_population(n: int, seed: int = 3, part_per_winding: int = 360):
                         agcct4_winding_number=wa[1], agcct5_winding_number=wa[2],
                         part_per_winding=part_per_winding))
     return out
+
+
+# ---------------------------------------------------------------- builders (this package's classes)
+def build_single_dipole():
+    """(trajectory, CCT) of the single-dipole workload."""
+    from .geometry import P2, Trajectory
+    from .magnets import CCT
+    c = SINGLE_DIPOLE
+    traj = (Trajectory.set_start_point(P2()).first_line(P2.x_direct(), c["drift"])
+            .add_arc_line(c["big_r"], c["clockwise"], c["bending_angle"]))
+    sign = -1.0 if c["clockwise"] else 1.0
+    cct = CCT.create_cct_along(traj, c["drift"], c["big_r"], c["small_r"], c["bending_angle"], c["tilt_angles"],
+                               c["winding_number"], c["current"], P2(0.0, 0.0),
+                               P2(2 * math.pi * c["winding_number"], sign * c["bending_angle"] / 180.0 * math.pi),
+                               c["disperse_number_per_winding"])
+    return traj, cct
+
+
+def single_dipole_particles(n: int = 32, seed: int = 0) -> np.ndarray:
+    """(n, 10) proton records at the start of the single-dipole arc."""
+    from .particles import ParticleFactory, PhaseSpaceParticle, particles_to_array
+    c = SINGLE_DIPOLE
+    traj, _ = build_single_dipole()
+    ideal = ParticleFactory.create_proton_along(traj, c["drift"], c["kinetic_MeV"])
+    pss = uniform_ellipse_phase_space(n, seed)
+    ps = ParticleFactory.create_from_phase_space_particles(
+        ideal, ideal.get_natural_coordinate_system(), [PhaseSpaceParticle(*map(float, r)) for r in pss])
+    return particles_to_array(ps)
+
+
+def build_gantry_section(**overrides):
+    """HUST second bending section with the gantry-section workload's parameters."""
+    from .beamline import HUST_SC_GANTRY
+    g = GANTRY_SECTION
+    kw = dict(agcct345_tilt_angles=g["agcct345_tilt_angles"], agcct345_current=g["agcct345_current"],
+              part_per_winding=g["part_per_winding"])
+    kw.update(overrides)
+    return HUST_SC_GANTRY(**kw).create_second_bending_part_beamline()
+
+
+def beam_particles(bl, n: int, seed: int, kinetic_MeV: float, gaussian: bool = True) -> np.ndarray:
+    """(n, 10) proton records at the start of beamline `bl`."""
+    from .particles import ParticleFactory, PhaseSpaceParticle, particles_to_array
+    ideal = ParticleFactory.create_proton_along(bl, 0.0, kinetic_MeV)
+    pss = gaussian_phase_space(n, seed) if gaussian else uniform_ellipse_phase_space(n, seed)
+    ps = ParticleFactory.create_from_phase_space_particles(
+        ideal, ideal.get_natural_coordinate_system(), [PhaseSpaceParticle(*map(float, r)) for r in pss])
+    return particles_to_array(ps)

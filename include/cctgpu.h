@@ -120,6 +120,18 @@ int cct_track(const double *d_kls, const double *d_p0s, const int64_t *d_seg_off
               double distance, double footstep, int32_t precision,
               void *d_scratch, int64_t scratch_bytes, void *stream);
 
+/* Measures the device's fused multiply-add pipe peak (flop/s, 2 per FMA) with
+ * independent FMA chains on every SM: fp64 = 0 for the FP32 pipe, 1 for FP64.
+ * These are the roofline denominators of the field kernels.  Synchronous. */
+int cct_probe_fma_peak(int fp64, double *flops_per_s);
+
+/* Test hook for failure detection without a GPU fault: makes every tracking
+ * grid barrier expect `phantom_blocks` extra CTAs that never arrive, and sets
+ * the barrier wait limit to `wait_ms` (<= 0 restores the 60 s default).  A
+ * tracking call then returns CCT_ERR_TIMEOUT after about wait_ms and the
+ * context stays usable.  Process-wide; not for production use. */
+int cct_test_set_barrier_fault(int phantom_blocks, int wait_ms);
+
 #ifdef __cplusplus
 }
 #endif

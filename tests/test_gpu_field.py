@@ -1,0 +1,177 @@
+"""Field-at-points parity on the GPU (FP64 drop-in and FP32-compensated form) against
+the reference's own outputs (golden fixtures) and the CPU oracle."""
+import math
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+from cctpy_gb300 import GPU_ACCELERATOR, HUST_SC_GANTRY, P3, engine, workloads as W
+from oracle import cct_oracle as O
+from tests.conftest import oracle_records
+
+F64_RTOL = 1e-12      # FP64 vs the reference FP64 CPU sum (norm-wise relative)
+F32C_RTOL = 1e-7      # FP32-compensated vs FP64 (the tolerance the FP32 form is built to)
+
+
+def rel(a, b):
+    return np.linalg.norm(a - b, axis=-1) / np.linalg.norm(b, axis=-1)
+
+
+@pytest.fixture(scope="module")
+def dipole():
+    _, cct = W.build_single_dipole()
+    return cct
+
+
+def test_f64_single_dipole_vs_reference(golden, dipole):
+    B = dipole.magnetic_field_at_points(golden["sd_field_pts"], "f64")
+    assert rel(B, golden["sd_field_B"]).max() < F64_RTOL
+
+
+def test_f32c_single_dipole_vs_reference(golden, dipole):
+    B = dipole.magnetic_field_at_points(golden["sd_field_pts"], "f32c")
+    assert rel(B, golden["sd_field_B"]).max() < F32C_RTOL
+
+
+def test_field_map_sample_f32c_vs_f64(dipole):
+    pts = W.field_map_points(1 << 16, seed=1)
+    b64 = dipole.magnetic_field_at_points(pts, "f64")
+    b32 = dipole.magnetic_field_at_points(pts, "f32c")
+    e = rel(b32, b64)
+    assert e.max() < F32C_RTOL and np.sqrt((e ** 2).mean()) < F32C_RTOL / 3
+
+
+def test_single_point_api_matches_batch(golden, dipole):
+    p = golden["sd_field_pts"][3]
+    b = dipole.magnetic_field_at(P3(*p))
+    assert rel(np.array(b.to_list()), golden["sd_field_B"][3]) < F64_RTOL
+
+
+@pytest.mark.parametrize("prec,tol", [("f64", F64_RTOL), ("f32c", F32C_RTOL)])
+def test_hust2_beamline_with_qs(golden, prec, tol):
+    bl = HUST_SC_GANTRY().create_second_bending_part_beamline()     # 119 520 segments: ragged last tile
+    B = bl.magnetic_field_at_points(golden["h2_field_pts"], prec)
+    assert rel(B, golden["h2_field_B"]).max() < tol
+
+
+@pytest.mark.parametrize("prec,tol", [("f64", F64_RTOL), ("f32c", F32C_RTOL)])
+def test_gantry_section_vs_reference(golden, prec, tol):
+    bl = W.build_gantry_section()
+    B = bl.magnetic_field_at_points(golden["gs_field_pts"], prec)
+    assert rel(B, golden["gs_field_B"]).max() < tol
+
+
+def test_qs_known_answer_bitwise(golden, records_json):
+    ga = GPU_ACCELERATOR(GPU_ACCELERATOR.FLOAT64)
+    rec = oracle_records(records_json["qs_known"])[0]
+    data = O.QSOracle(rec).to_array()
+    for p, want in zip(golden["qs_pts"], golden["qs_B"]):
+        got = ga.magnet_at_qs(data, P3(*p)).to_list()
+        assert got == want.tolist()
+    # gpu_accelerator.py:1219, printed known answer
+    assert ga.magnet_at_qs(data, P3(0.95, 0, 0)).to_list() == [0.0, 0.0, 0.27500000000000024]
+
+
+def test_qs_beamline_known_answer(golden, records_json):
+    recs = oracle_records(records_json["qs_beamline"])
+    from cctpy_gb300 import Beamline, P2, MM
+    bl = (Beamline.set_start_point(P2()).first_drift(P2.x_direct(), 1)
+          .append_qs(0.27, 5, 20, 100 * MM).append_drift(1)
+          .append_dipole_cct(1, 100 * MM, 120 * MM, 45, [30], 60, 10000).append_drift(1))
+    for prec, tol in (("f64", F64_RTOL), ("f32c", F32C_RTOL)):
+        B = bl.magnetic_field_at_points(golden["qsbl_pts"], prec)
+        assert rel(B, golden["qsbl_B"]).max() < tol
+    ga = GPU_ACCELERATOR(GPU_ACCELERATOR.FLOAT64)
+    b = ga.magnet_at_beamline_with_single_qs(bl, P3(2.3, 50 * MM, 0)).to_list()
+    # gpu_accelerator.py:1374 (printed by an earlier revision; ~5e-14 T away today)
+    assert np.allclose(b, [-0.021273493843574243, 0.048440921145815385, 1.0980479752081713], rtol=0, atol=1e-13)
+
+
+def test_single_element_known_answer():
+    # codes/tests/cuda_test.py:99-109: kl = p1 - p0, midpoint, field point at the origin
+    ga = GPU_ACCELERATOR(GPU_ACCELERATOR.FLOAT64)
+    b = ga.current_element_B(np.array([0.1, 0.2, 0.3]), np.array([1.05, 1.1, 1.15]), 1, P3(0, 0, 0)).to_list()
+    assert np.allclose(b, [0.014429237347383132, -0.028858474694766215, 0.01442923734738309], rtol=1e-13)
+
+
+def test_solenoid_known_answers():
+    # codes/tests/sole_layer_cct_test.py:14-43 (I = 1000 A; 1e-7 I folded into kl)
+    n, pas, r, L = 20, 360, 0.01, 0.1
+    ts = np.linspace(0, n * 2 * np.pi, n * pas)
+    path = np.array([[r * np.sin(t), r * np.cos(t), t / (n * 2 * np.pi) * L] for t in ts])
+    kl = (1e-7 * 1000 * (path[1:] - path[:-1])).reshape(-1)
+    p0 = (0.5 * (path[1:] + path[:-1])).reshape(-1)
+    want = [([0, 0, 0], [-9.641213222579932E-5, -0.0016659990498348225, -0.1250432833225887]),
+            ([0, 0, 0.05], [-7.496745957474563E-4, -3.7777669447541795E-19, -0.24645342280018406]),
+            ([0, 0.001, 0.05], [-7.128547526957852E-4, -6.352747104407253E-20, -0.2464630712060889])]
+    for prec in (GPU_ACCELERATOR.FLOAT64, GPU_ACCELERATOR.FLOAT32):
+        ga = GPU_ACCELERATOR(prec)
+        tol = 1e-10 if prec == GPU_ACCELERATOR.FLOAT64 else 1e-7
+        for p, b in want:
+            got = ga.current_element_B(kl, p0, len(ts) - 1, P3(*p)).to_list()
+            assert np.allclose(got, b, rtol=tol, atol=tol * 0.25)
+
+
+def test_edge_cases(dipole):
+    ds = engine.design_of(dipole)
+    # empty point set
+    assert engine.field_at_points(ds, np.zeros((0, 3)), "f64").shape == (0, 3)
+    assert engine.field_at_points(ds, np.zeros((0, 3)), "f32c").shape == (0, 3)
+    # point counts that are not multiples of the CTA size
+    pts = W.field_map_points(517, seed=9)
+    b64 = engine.field_at_points(ds, pts, "f64")
+    b32 = engine.field_at_points(ds, pts, "f32c")
+    assert rel(b32, b64).max() < F32C_RTOL
+    # a design without segments (QS only) and one with a few segments (single ragged tile)
+    from cctpy_gb300 import QS, LocalCoordinateSystem, MM
+    qs = QS(LocalCoordinateSystem(P3(1, 0, 0), -P3.x_direct(), P3.y_direct()), 0.27, 5, 20, 100 * MM)
+    small = engine.DesignSet([engine.host_design([qs]),
+                              (np.array([[1e-4, 2e-4, 3e-4]] * 5), np.random.default_rng(0).random((5, 3)),
+                               np.zeros((0, 16)))])
+    q = np.array([[0.95, 0.0, 0.0], [0.97, 0.1, 0.02]])
+    for prec in ("f64", "f32c"):
+        b = engine.field_at_points(small, q, prec, design=0)
+        assert b[0].tolist() == [0.0, 0.0, 0.27500000000000024]
+        b1 = engine.field_at_points(small, q, prec, design=1)
+        ref = np.array([O.segments_field_local(np.array([[1e-4, 2e-4, 3e-4]] * 5),
+                                               np.random.default_rng(0).random((5, 3)), tuple(x)) for x in q])
+        assert rel(b1, ref).max() < (1e-12 if prec == "f64" else 1e-6)
+    # rejected inputs
+    with pytest.raises(ValueError):
+        engine.field_at_points(ds, np.zeros((4, 2)), "f64")
+    with pytest.raises(ValueError):
+        engine.field_at_points(ds, np.zeros((4, 3)), "bf16")
+
+
+def test_multi_design_packed_f32c(golden, dipole):
+    bl = HUST_SC_GANTRY().create_second_bending_part_beamline()
+    ds = engine.design_set_of([dipole, bl])
+    b0 = engine.field_at_points(ds, golden["sd_field_pts"], "f32c", design=0)
+    b1 = engine.field_at_points(ds, golden["h2_field_pts"], "f32c", design=1)
+    assert rel(b0, golden["sd_field_B"]).max() < F32C_RTOL
+    assert rel(b1, golden["h2_field_B"]).max() < F32C_RTOL
+
+
+def test_torch_device_io(dipole):
+    pts = torch.from_numpy(W.field_map_points(1000, seed=4)).cuda()
+    out = engine.field_at_points(engine.design_of(dipole), pts, "f32c")
+    assert isinstance(out, torch.Tensor) and out.is_cuda and out.shape == (1000, 3)
+
+
+def test_host_buffer_entry_point(golden, dipole):
+    import ctypes
+    from cctpy_gb300 import _lib
+    lib = _lib.load()
+    kl, p0 = dipole.global_segments()
+    kl, p0 = np.ascontiguousarray(kl), np.ascontiguousarray(p0)
+    pts = np.ascontiguousarray(golden["sd_field_pts"])
+    for prec, tol in ((0, F64_RTOL), (1, F32C_RTOL)):
+        out = np.zeros_like(pts)
+        rc = lib.cct_field_host(kl.ctypes.data, p0.ctypes.data, kl.shape[0], None, 0, pts.ctypes.data,
+                                pts.shape[0], out.ctypes.data, prec)
+        _lib.check(rc, "cct_field_host")
+        assert rel(out, golden["sd_field_B"]).max() < tol

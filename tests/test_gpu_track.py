@@ -1,0 +1,128 @@
+"""RK4 tracking parity on the GPU against particles tracked by the reference itself
+(golden fixtures) and the CPU oracle, plus the accelerator API conventions and the
+failure paths (bounded barrier wait, non-finite state)."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+from cctpy_gb300 import (GPU_ACCELERATOR, HUST_SC_GANTRY, ParticleRunner, RunningParticle, engine,
+                         workloads as W, _lib)
+from cctpy_gb300.particles import particles_to_array
+from oracle import cct_oracle as O
+from tests.conftest import oracle_records
+
+POS_TOL_F64 = 1e-9      # m, FP64 GPU vs reference FP64 CPU after the whole track
+VEL_RTOL_F64 = 1e-9
+POS_TOL_F32C = 1e-6     # m (1 um), FP32-compensated vs reference FP64
+
+
+def check(out, want, pos_tol, vel_rtol):
+    assert np.abs(out[:, 0:3] - want[:, 0:3]).max() < pos_tol
+    assert (np.abs(out[:, 3:6] - want[:, 3:6]).max() / np.abs(want[:, 3:6]).max()) < vel_rtol
+    assert np.array_equal(out[:, 6:9], want[:, 6:9])
+    np.testing.assert_allclose(out[:, 9], want[:, 9], rtol=1e-15)
+
+
+@pytest.mark.parametrize("prec,ptol,vtol", [("f64", POS_TOL_F64, VEL_RTOL_F64), ("f32c", POS_TOL_F32C, 1e-6)])
+def test_single_dipole_32_protons(golden, prec, ptol, vtol):
+    _, cct = W.build_single_dipole()
+    out = engine.track(engine.design_of(cct), golden["sd_particles_in"], W.single_dipole_track_length(), 0.001,
+                       prec)[0]
+    check(out, golden["sd_particles_out"], ptol, vtol)
+
+
+@pytest.mark.parametrize("prec,ptol,vtol", [("f64", POS_TOL_F64, VEL_RTOL_F64), ("f32c", POS_TOL_F32C, 1e-6)])
+def test_hust2_section_with_qs(golden, prec, ptol, vtol):
+    bl = HUST_SC_GANTRY().create_second_bending_part_beamline()
+    out = engine.track(engine.design_of(bl), golden["h2_particles_in"], float(golden["h2_length"][0]), 0.1,
+                       prec)[0]
+    check(out, golden["h2_particles_out"], ptol, vtol)
+
+
+@pytest.mark.parametrize("prec,ptol,vtol", [("f64", POS_TOL_F64, VEL_RTOL_F64), ("f32c", POS_TOL_F32C, 1e-6)])
+def test_gantry_section(golden, prec, ptol, vtol):
+    bl = W.build_gantry_section()
+    out = engine.track(engine.design_of(bl), golden["gs_particles_in"], 3.5, 0.05, prec)[0]
+    check(out, golden["gs_particles_out"], ptol, vtol)
+
+
+@pytest.mark.parametrize("prec,ptol,vtol", [("f64", POS_TOL_F64, VEL_RTOL_F64), ("f32c", POS_TOL_F32C, 1e-6)])
+def test_design_population_one_launch(golden, prec, ptol, vtol):
+    bls = [HUST_SC_GANTRY(**kw).create_second_bending_part_beamline() for kw in W.design_population(2, seed=3)]
+    ds = engine.design_set_of(bls)
+    L = float(golden["dp0_length"][0])
+    assert abs(L - float(golden["dp1_length"][0])) < 1e-12
+    parts = np.stack([golden["dp0_particles_in"], golden["dp1_particles_in"]])
+    out = engine.track(ds, parts, L, 0.05, prec)
+    for d in range(2):
+        check(out[d], golden[f"dp{d}_particles_out"], ptol, vtol)
+
+
+def test_ragged_particle_counts_match_oracle(records_json):
+    # 37 particles: one full group of 32 and a ragged group of 5; short track, oracle in seconds
+    bl = HUST_SC_GANTRY().create_second_bending_part_beamline()
+    ps = W.beam_particles(bl, 37, seed=5, kinetic_MeV=215.0)
+    out = engine.track(engine.design_of(bl), ps, 0.6, 0.1, "f64")[0]
+    ob = O.BeamlineOracle(oracle_records(records_json["hust2_default"]))
+    for i in (0, 31, 32, 36):
+        want = O.rk4_track(ps[i], ob.field_at, 0.6, 0.1)
+        assert np.abs(out[i, :3] - want[:3]).max() < 1e-11
+
+
+def test_accelerator_conventions(golden):
+    bl = HUST_SC_GANTRY().create_second_bending_part_beamline()
+    ps = [RunningParticle.from_numpy_array_data(r) for r in golden["h2_particles_in"]]
+    L = float(golden["h2_length"][0])
+    ga = GPU_ACCELERATOR(GPU_ACCELERATOR.FLOAT64, block_dim_x=512)
+    before = particles_to_array(ps)
+    res = ga.track_multi_particle_beamline_for_magnet_with_multi_qs([bl, bl], ps, L, 0.1)
+    assert np.array_equal(particles_to_array(ps), before)          # inputs untouched
+    assert len(res) == 2 and len(res[0]) == 4
+    check(particles_to_array(res[1]), golden["h2_particles_out"], POS_TOL_F64, VEL_RTOL_F64)
+    one = ps[0].copy()
+    ga.track_one_particle_with_multi_qs(bl, one, L, 0.1)             # in place
+    check(particles_to_array([one]), golden["h2_particles_out"][:1], POS_TOL_F64, VEL_RTOL_F64)
+    many = [p.copy() for p in ps]
+    ParticleRunner.run_only(many, bl, L, 0.1)
+    check(particles_to_array(many), golden["h2_particles_out"], POS_TOL_F64, VEL_RTOL_F64)
+    with pytest.raises(ValueError):
+        GPU_ACCELERATOR(block_dim_x=1000)
+    with pytest.raises(ValueError):
+        GPU_ACCELERATOR(GPU_ACCELERATOR.FLOAT32, max_current_element_number=1000).track_one_particle_with_multi_qs(
+            bl, ps[0].copy(), L, 0.1)
+
+
+def test_phase_ellipse_api():
+    bl = HUST_SC_GANTRY().create_second_bending_part_beamline()
+    ga = GPU_ACCELERATOR(GPU_ACCELERATOR.FLOAT32)
+    res = ga.track_phase_ellipse_in_multi_beamline([bl], 3.5, 7.5, 3.5, 7.5, 0.0, 4, 215, length=1.0, footstep=0.05)
+    assert len(res) == 1 and len(res[0][0]) == 4 and len(res[0][1]) == 4
+
+
+def test_bounded_barrier_wait_reports_timeout(golden):
+    """A barrier that can never complete (phantom CTAs that never arrive) gives up after
+    the wait limit and reports CCT_ERR_TIMEOUT; the context stays usable afterwards."""
+    _, cct = W.build_single_dipole()
+    ds = engine.design_of(cct)
+    lib = _lib.load()
+    lib.cct_test_set_barrier_fault(1, 300)
+    try:
+        with pytest.raises(_lib.CctTimeoutError):
+            engine.track(ds, golden["sd_particles_in"][:2], 0.01, 0.001, "f32c")
+    finally:
+        lib.cct_test_set_barrier_fault(0, 0)
+    out = engine.track(ds, golden["sd_particles_in"][:2], 0.01, 0.001, "f64")
+    assert np.isfinite(out).all()
+
+
+def test_nonfinite_particle_is_reported(golden):
+    _, cct = W.build_single_dipole()
+    ps = golden["sd_particles_in"][:3].copy()
+    ps[1, 3] = np.nan
+    with pytest.raises(_lib.CctNonFiniteError):
+        engine.track(engine.design_of(cct), ps, 0.01, 0.001, "f64")
+    with pytest.raises(ValueError):
+        engine.track(engine.design_of(cct), ps, -1.0, 0.001, "f64")
