@@ -10,8 +10,8 @@ namespace cctgpu {
 
 // ---------------------------------------------------------------- constants
 constexpr int kTile = 128;                   // segments per FP32c tile
-constexpr int kTileHeaderBytes = 32;         // FP64 origin (x, y, z) + pad
-constexpr int kTileBytes = kTileHeaderBytes + 6 * kTile * 4;   // 3104, a multiple of 16
+constexpr int kTileHeaderBytes = 32;         // double-float origin (x, y, z), count, pad
+constexpr int kTileBytes = kTileHeaderBytes + 9 * kTile * 4;   // 4640, a multiple of 16
 constexpr int kPackedHeaderBytes = 256;      // magic, n_designs, n_tiles
 constexpr int64_t kPackedMagic = 0x4343543332434331LL;          // "CCT32CC1"
 constexpr float kPadOffset = 1.0e18f;        // padding segment: kl = 0, far away

@@ -20,8 +20,32 @@ __global__ void __launch_bounds__(256) fma_chain_kernel(T *out, int iters, T a, 
     if (s == (T)12345.678) out[0] = s;   // keeps the chains live; never true for these inputs
 }
 
+// Packed FP32x2 chains (two FP32 FMAs per instruction).
+__global__ void __launch_bounds__(256) fma2_chain_kernel(float *out, int iters, float a, float b) {
+    uint64_t x[8], av, bv;
+    asm("mov.b64 %0, {%1, %1};" : "=l"(av) : "f"(a));
+    asm("mov.b64 %0, {%1, %1};" : "=l"(bv) : "f"(b));
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        const float v = (float)(threadIdx.x + i) * 1e-3f;
+        asm("mov.b64 %0, {%1, %2};" : "=l"(x[i]) : "f"(v), "f"(v + 0.5f));
+    }
+    for (int it = 0; it < iters; ++it) {
+#pragma unroll
+        for (int i = 0; i < 8; ++i) asm("fma.rn.f32x2 %0, %0, %1, %2;" : "+l"(x[i]) : "l"(av), "l"(bv));
+    }
+    float s = 0.0f;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        float lo, hi;
+        asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(x[i]));
+        s += lo + hi;
+    }
+    if (s == 12345.678f) out[0] = s;
+}
+
 template <typename T>
-static int probe(double *flops_per_s, int iters) {
+static int probe(double *flops_per_s, int iters, bool packed = false) {
     int dev = 0, sms = 0;
     CCT_TRY_CUDA(cudaGetDevice(&dev));
     CCT_TRY_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
@@ -31,11 +55,17 @@ static int probe(double *flops_per_s, int iters) {
     CCT_TRY_CUDA(cudaEventCreate(&e0));
     CCT_TRY_CUDA(cudaEventCreate(&e1));
     const int grid = sms * 8;
-    fma_chain_kernel<T><<<grid, 256>>>(out, iters / 8, (T)0.999999, (T)1e-7);   // warm-up
+    auto launch = [&](int n) {
+        if (packed)
+            fma2_chain_kernel<<<grid, 256>>>(reinterpret_cast<float *>(out), n, 0.999999f, 1e-7f);
+        else
+            fma_chain_kernel<T><<<grid, 256>>>(out, n, (T)0.999999, (T)1e-7);
+    };
+    launch(iters / 8);   // warm-up
     float best = 1e30f;
     for (int rep = 0; rep < 3; ++rep) {
         CCT_TRY_CUDA(cudaEventRecord(e0));
-        fma_chain_kernel<T><<<grid, 256>>>(out, iters, (T)0.999999, (T)1e-7);
+        launch(iters);
         CCT_TRY_CUDA(cudaEventRecord(e1));
         CCT_TRY_CUDA(cudaEventSynchronize(e1));
         float ms = 0;
@@ -45,14 +75,16 @@ static int probe(double *flops_per_s, int iters) {
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     cudaFree(out);
-    *flops_per_s = 2.0 * 8.0 * (double)iters * (double)grid * 256.0 / (best * 1e-3);
+    *flops_per_s = (packed ? 2.0 : 1.0) * 2.0 * 8.0 * (double)iters * (double)grid * 256.0 / (best * 1e-3);
     return CCT_OK;
 }
 
 }  // namespace cctgpu
 
-extern "C" int cct_probe_fma_peak(int fp64, double *flops_per_s) {
+extern "C" int cct_probe_fma_peak(int kind, double *flops_per_s) {
     cctgpu::clear_error();
     if (!flops_per_s) return cctgpu::set_error(CCT_ERR_ARG, "null output");
-    return fp64 ? cctgpu::probe<double>(flops_per_s, 1 << 12) : cctgpu::probe<float>(flops_per_s, 1 << 16);
+    if (kind == 1) return cctgpu::probe<double>(flops_per_s, 1 << 12);
+    if (kind == 2) return cctgpu::probe<float>(flops_per_s, 1 << 15, true);
+    return cctgpu::probe<float>(flops_per_s, 1 << 16);
 }

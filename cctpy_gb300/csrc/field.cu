@@ -7,11 +7,13 @@
 //  * field_f64_kernel   plain FP64, one thread per field point (x2), segment tiles staged in
 //                       shared memory by the CTA; the drop-in for CCT.magnetic_field_at.
 //  * field_f32c_kernel  FP32 arithmetic on per-tile local offsets: each tile of 128 segments
-//                       carries an FP64 origin, the point-minus-origin subtraction is FP64,
-//                       the 128 pair terms run in FP32 (rsqrt on the MUFU pipe) summed in
-//                       sub-blocks of 32 with a Kahan-compensated tile partial, and tile
-//                       partials accumulate in FP64.  Tiles are streamed into shared memory
-//                       by the TMA bulk-copy engine through a 4-deep mbarrier ring.
+//                       carries a double-float origin, point-minus-origin is taken in
+//                       double-float, the pair terms run as packed FP32x2 (two segments
+//                       per instruction; rsqrt on the MUFU pipe), summed in FP32 over
+//                       sub-blocks of 64 segments into a Kahan-compensated (S, C) pair
+//                       resolved in FP64 at the end (tile.cuh).  Tiles are streamed into
+//                       shared memory by the TMA bulk-copy engine through a 4-deep
+//                       mbarrier ring.
 #include <cstdarg>
 #include <cstdio>
 #include <vector>
@@ -108,10 +110,9 @@ int launch_field_f64(const double *kls, const double *p0s, int64_t n_seg, const 
 }
 
 // ===================================================================== FP32c pack
-// Tile layout (kTileBytes = 3104, 16-byte multiple):
-//   double origin[3]; double count;          (32 B)
-//   float kx[128], ky[128], kz[128];         kl components
-//   float px[128], py[128], pz[128];         p0 - origin
+// Packs FP64 segments into FP32c tiles (layout in tile.cuh).  The tile origin is the
+// centroid of the tile's midpoints rounded to a double-float (hi, lo) pair; offsets are
+// taken from that represented origin, so point - origin needs no FP64 in the kernels.
 __global__ void __launch_bounds__(kTile) pack_f32c_kernel(const double *__restrict__ kls,
                                                           const double *__restrict__ p0s,
                                                           unsigned char *__restrict__ packed) {
@@ -150,30 +151,40 @@ __global__ void __launch_bounds__(kTile) pack_f32c_kernel(const double *__restri
         }
         __syncthreads();
     }
+    float ohi[3], olo[3];
     double o[3];
 #pragma unroll
-    for (int c = 0; c < 3; ++c) o[c] = cnt > 0 ? red[c][0] / cnt : 0.0;
+    for (int c = 0; c < 3; ++c) {
+        split_df(cnt > 0 ? red[c][0] / cnt : 0.0, ohi[c], olo[c]);
+        o[c] = (double)ohi[c] + (double)olo[c];
+    }
 
     unsigned char *tile = tiles + t * (int64_t)kTileBytes;
-    double *hdr = reinterpret_cast<double *>(tile);
+    TileHeader *hdr = reinterpret_cast<TileHeader *>(tile);
     float *f = reinterpret_cast<float *>(tile + kTileHeaderBytes);
     if (i == 0) {
-        hdr[0] = o[0];
-        hdr[1] = o[1];
-        hdr[2] = o[2];
-        hdr[3] = (double)cnt;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            hdr->o_hi[c] = ohi[c];
+            hdr->o_lo[c] = olo[c];
+        }
+        hdr->count = cnt;
+        hdr->pad = 0;
     }
     if (i < cnt) {
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
-            f[c * kTile + i] = (float)k[c];
-            f[(3 + c) * kTile + i] = (float)(p[c] - o[c]);
+            const float kf = (float)k[c];
+            f[c * kTile + i] = kf;
+            f[(3 + c) * kTile + i] = -kf;
+            f[(6 + c) * kTile + i] = (float)(p[c] - o[c]);
         }
-    } else {
+    } else {   // padding: zero current element far away (contributes exactly 0)
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
             f[c * kTile + i] = 0.0f;
-            f[(3 + c) * kTile + i] = kPadOffset;
+            f[(3 + c) * kTile + i] = 0.0f;
+            f[(6 + c) * kTile + i] = kPadOffset;
         }
     }
 }
@@ -250,16 +261,16 @@ __global__ void __launch_bounds__(kF32Block, 2) field_f32c_kernel(const unsigned
         }
     }
 
-    double px[kF32Ppt], py[kF32Ppt], pz[kF32Ppt], bx[kF32Ppt], by[kF32Ppt], bz[kF32Ppt];
+    float ph[kF32Ppt][3], pl[kF32Ppt][3];
 #pragma unroll
     for (int i = 0; i < kF32Ppt; ++i) {
         int64_t idx = base + tid + (int64_t)i * kF32Block;
         if (idx >= n) idx = n - 1;
-        px[i] = pts[3 * idx];
-        py[i] = pts[3 * idx + 1];
-        pz[i] = pts[3 * idx + 2];
-        bx[i] = by[i] = bz[i] = 0.0;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) split_df(pts[3 * idx + c], ph[i][c], pl[i][c]);
     }
+    F32cAcc<kF32Ppt> acc;
+    acc.zero();
 
     bool failed = false;
     for (int64_t t = 0; t < nt; ++t) {
@@ -276,7 +287,7 @@ __global__ void __launch_bounds__(kF32Block, 2) field_f32c_kernel(const unsigned
             cctdev::mbar_arrive_expect_tx(&full[sp], kTileBytes);
             cctdev::bulk_g2s(buf[sp], tiles + (t - 1 + kStages) * (int64_t)kTileBytes, kTileBytes, &full[sp]);
         }
-        tile_f32c<kF32Ppt>(buf[s], px, py, pz, bx, by, bz);
+        tile_f32c<kF32Ppt>(buf[s], ph, pl, acc);
     }
     if (failed) {
         // let copies still in flight land before the CTA's shared memory is released
@@ -294,10 +305,12 @@ __global__ void __launch_bounds__(kF32Block, 2) field_f32c_kernel(const unsigned
             B[3 * idx] = B[3 * idx + 1] = B[3 * idx + 2] = __longlong_as_double(0x7ff8000000000000LL);
             continue;
         }
-        for (int q = 0; q < n_qs; ++q) qs_field_add(qs + kQsRecord * q, px[i], py[i], pz[i], bx[i], by[i], bz[i]);
-        B[3 * idx] = bx[i];
-        B[3 * idx + 1] = by[i];
-        B[3 * idx + 2] = bz[i];
+        double bx = acc.total(i, 0), by = acc.total(i, 1), bz = acc.total(i, 2);
+        for (int q = 0; q < n_qs; ++q)
+            qs_field_add(qs + kQsRecord * q, pts[3 * idx], pts[3 * idx + 1], pts[3 * idx + 2], bx, by, bz);
+        B[3 * idx] = bx;
+        B[3 * idx + 1] = by;
+        B[3 * idx + 2] = bz;
     }
 }
 

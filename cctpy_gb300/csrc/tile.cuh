@@ -1,68 +1,143 @@
 // One FP32-compensated tile of the packed segment form, shared by the field-map and
 // tracking kernels.
+//
+// Tile (kTileBytes = 4640 = 16 * 290):
+//   float o_hi[3], o_lo[3];  int count; int pad;      origin = o_hi + o_lo (double-float)
+//   float kx[128], ky[128], kz[128];                   kl
+//   float nkx[128], nky[128], nkz[128];                -kl
+//   float px[128], py[128], pz[128];                   p0 - origin
+// Arithmetic: packed FP32 pairs (PTX f32x2, two segments per instruction) for every
+// multiply/add of the pair term; rsqrt on the MUFU pipe; each half accumulates its
+// segments in FP32 over a sub-block of 64 segments, the sub-block sum is added to a
+// Kahan-compensated (S, C) pair, and S - C is taken in FP64 at the end.
 #pragma once
+
+#include <stdint.h>
 
 #include "cctgpu_internal.cuh"
 
 namespace cctgpu {
 
-// Kahan-compensated accumulation of one 128-segment tile for PPT points; adds the tile
-// partial to the FP64 accumulators.  `tile` may point to shared or global memory.
+typedef uint64_t f2;   // two packed FP32 values (low half = even segment)
+
+__device__ __forceinline__ f2 f2_pack(float lo, float hi) {
+    f2 r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+    return r;
+}
+__device__ __forceinline__ void f2_unpack(f2 v, float &lo, float &hi) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+}
+__device__ __forceinline__ f2 f2_sub(f2 a, f2 b) {
+    f2 d;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ f2 f2_mul(f2 a, f2 b) {
+    f2 d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ f2 f2_fma(f2 a, f2 b, f2 c) {
+    f2 d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+__device__ __forceinline__ float rsqrt_mufu(float x) {
+    float y;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+// Kahan step: (S, C) += s
+__device__ __forceinline__ void kahan_add(float &S, float &C, float s) {
+    const float y = __fsub_rn(s, C);
+    const float t = __fadd_rn(S, y);
+    C = __fsub_rn(__fsub_rn(t, S), y);
+    S = t;
+}
+
+struct TileHeader {
+    float o_hi[3], o_lo[3];
+    int count, pad;
+};
+
+// Per-point state of the compensated sum.
 template <int PPT>
-__device__ __forceinline__ void tile_f32c(const unsigned char *tile, const double (&px)[PPT],
-                                          const double (&py)[PPT], const double (&pz)[PPT], double (&bx)[PPT],
-                                          double (&by)[PPT], double (&bz)[PPT]) {
-    const double *hdr = reinterpret_cast<const double *>(tile);
-    const float4 *f4 = reinterpret_cast<const float4 *>(tile + kTileHeaderBytes);
-    const double ox = hdr[0], oy = hdr[1], oz = hdr[2];
-    float qx[PPT], qy[PPT], qz[PPT];
-    float Sx[PPT], Sy[PPT], Sz[PPT], Cx[PPT], Cy[PPT], Cz[PPT];
+struct F32cAcc {
+    float S[PPT][3], C[PPT][3];
+    __device__ __forceinline__ void zero() {
 #pragma unroll
-    for (int i = 0; i < PPT; ++i) {
-        qx[i] = (float)(px[i] - ox);
-        qy[i] = (float)(py[i] - oy);
-        qz[i] = (float)(pz[i] - oz);
-        Sx[i] = Sy[i] = Sz[i] = Cx[i] = Cy[i] = Cz[i] = 0.0f;
+        for (int i = 0; i < PPT; ++i)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) S[i][c] = C[i][c] = 0.0f;
     }
+    __device__ __forceinline__ double total(int i, int c) const { return (double)S[i][c] - (double)C[i][c]; }
+};
+
+// Accumulate one tile for PPT points given as double-float (hi, lo) coordinates.
+template <int PPT>
+__device__ __forceinline__ void tile_f32c(const unsigned char *tile, const float (&ph)[PPT][3],
+                                          const float (&pl)[PPT][3], F32cAcc<PPT> &acc) {
+    const TileHeader *h = reinterpret_cast<const TileHeader *>(tile);
+    const ulonglong2 *v = reinterpret_cast<const ulonglong2 *>(tile + kTileHeaderBytes);
+    constexpr int Q = kTile / 4;   // ulonglong2 (4 floats) per component array
+    f2 q[PPT][3];
+#pragma unroll
+    for (int i = 0; i < PPT; ++i)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const float d = __fadd_rn(__fsub_rn(ph[i][c], h->o_hi[c]), __fsub_rn(pl[i][c], h->o_lo[c]));
+            q[i][c] = f2_pack(d, d);
+        }
 #pragma unroll 1
-    for (int sb = 0; sb < kTile / 32; ++sb) {
-        float sx[PPT], sy[PPT], sz[PPT];
+    for (int sb = 0; sb < kTile / 64; ++sb) {
+        f2 B[PPT][3];
 #pragma unroll
-        for (int i = 0; i < PPT; ++i) sx[i] = sy[i] = sz[i] = 0.0f;
-#pragma unroll 2
-        for (int j4 = sb * 8; j4 < sb * 8 + 8; ++j4) {
-            const float4 KX = f4[0 * (kTile / 4) + j4], KY = f4[1 * (kTile / 4) + j4], KZ = f4[2 * (kTile / 4) + j4];
-            const float4 PX = f4[3 * (kTile / 4) + j4], PY = f4[4 * (kTile / 4) + j4], PZ = f4[5 * (kTile / 4) + j4];
-            const float kx[4] = {KX.x, KX.y, KX.z, KX.w}, ky[4] = {KY.x, KY.y, KY.z, KY.w};
-            const float kz[4] = {KZ.x, KZ.y, KZ.z, KZ.w}, ox4[4] = {PX.x, PX.y, PX.z, PX.w};
-            const float oy4[4] = {PY.x, PY.y, PY.z, PY.w}, oz4[4] = {PZ.x, PZ.y, PZ.z, PZ.w};
+        for (int i = 0; i < PPT; ++i) B[i][0] = B[i][1] = B[i][2] = 0ull;
+#pragma unroll 1
+        for (int j = sb * 16; j < sb * 16 + 16; ++j) {          // 4 segments per iteration
+            const ulonglong2 KX = v[0 * Q + j], KY = v[1 * Q + j], KZ = v[2 * Q + j];
+            const ulonglong2 NX = v[3 * Q + j], NY = v[4 * Q + j], NZ = v[5 * Q + j];
+            const ulonglong2 PX = v[6 * Q + j], PY = v[7 * Q + j], PZ = v[8 * Q + j];
 #pragma unroll
-            for (int u = 0; u < 4; ++u) {
+            for (int hh = 0; hh < 2; ++hh) {
+                const f2 kx = hh ? KX.y : KX.x, ky = hh ? KY.y : KY.x, kz = hh ? KZ.y : KZ.x;
+                const f2 nx = hh ? NX.y : NX.x, ny = hh ? NY.y : NY.x, nz = hh ? NZ.y : NZ.x;
+                const f2 px = hh ? PX.y : PX.x, py = hh ? PY.y : PY.x, pz = hh ? PZ.y : PZ.x;
 #pragma unroll
                 for (int i = 0; i < PPT; ++i) {
-                    const float rx = qx[i] - ox4[u], ry = qy[i] - oy4[u], rz = qz[i] - oz4[u];
-                    const float inv = rsqrtf(fmaf(rx, rx, fmaf(ry, ry, rz * rz)));
-                    const float inv3 = inv * inv * inv;
-                    sx[i] = fmaf(fmaf(ky[u], rz, -kz[u] * ry), inv3, sx[i]);
-                    sy[i] = fmaf(fmaf(kz[u], rx, -kx[u] * rz), inv3, sy[i]);
-                    sz[i] = fmaf(fmaf(kx[u], ry, -ky[u] * rx), inv3, sz[i]);
+                    const f2 rx = f2_sub(q[i][0], px), ry = f2_sub(q[i][1], py), rz = f2_sub(q[i][2], pz);
+                    const f2 r2 = f2_fma(rx, rx, f2_fma(ry, ry, f2_mul(rz, rz)));
+                    float a, b;
+                    f2_unpack(r2, a, b);
+                    const f2 inv = f2_pack(rsqrt_mufu(a), rsqrt_mufu(b));
+                    const f2 inv3 = f2_mul(f2_mul(inv, inv), inv);
+                    // kl x r = (ky rz - kz ry, kz rx - kx rz, kx ry - ky rx)
+                    const f2 cx = f2_fma(ky, rz, f2_mul(nz, ry));
+                    const f2 cy = f2_fma(kz, rx, f2_mul(nx, rz));
+                    const f2 cz = f2_fma(kx, ry, f2_mul(ny, rx));
+                    B[i][0] = f2_fma(cx, inv3, B[i][0]);
+                    B[i][1] = f2_fma(cy, inv3, B[i][1]);
+                    B[i][2] = f2_fma(cz, inv3, B[i][2]);
                 }
             }
         }
 #pragma unroll
-        for (int i = 0; i < PPT; ++i) {   // Kahan step: S += s with compensation C
-            float y, t;
-            y = __fsub_rn(sx[i], Cx[i]); t = __fadd_rn(Sx[i], y); Cx[i] = __fsub_rn(__fsub_rn(t, Sx[i]), y); Sx[i] = t;
-            y = __fsub_rn(sy[i], Cy[i]); t = __fadd_rn(Sy[i], y); Cy[i] = __fsub_rn(__fsub_rn(t, Sy[i]), y); Sy[i] = t;
-            y = __fsub_rn(sz[i], Cz[i]); t = __fadd_rn(Sz[i], y); Cz[i] = __fsub_rn(__fsub_rn(t, Sz[i]), y); Sz[i] = t;
-        }
-    }
+        for (int i = 0; i < PPT; ++i)
 #pragma unroll
-    for (int i = 0; i < PPT; ++i) {
-        bx[i] += (double)Sx[i] - (double)Cx[i];
-        by[i] += (double)Sy[i] - (double)Cy[i];
-        bz[i] += (double)Sz[i] - (double)Cz[i];
+            for (int c = 0; c < 3; ++c) {
+                float lo, hi;
+                f2_unpack(B[i][c], lo, hi);
+                kahan_add(acc.S[i][c], acc.C[i][c], __fadd_rn(lo, hi));
+            }
     }
+}
+
+// Split an FP64 coordinate into a double-float (hi, lo) pair.
+__device__ __forceinline__ void split_df(double x, float &hi, float &lo) {
+    hi = (float)x;
+    lo = (float)(x - (double)hi);
 }
 
 }  // namespace cctgpu

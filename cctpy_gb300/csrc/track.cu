@@ -130,8 +130,17 @@ __device__ void unit_field(const TrackParams &P, int64_t u, double (*red)[32][3]
     const int64_t t_beg = c * ct, t_end = min(nt, (c + 1) * ct);
     if (P.precision == 1) {
         const unsigned char *tiles = P.tiles + P.tile_off[d] * (int64_t)kTileBytes;
+        float ph[1][3], pl[1][3];
+        split_df(px[0], ph[0][0], pl[0][0]);
+        split_df(py[0], ph[0][1], pl[0][1]);
+        split_df(pz[0], ph[0][2], pl[0][2]);
+        F32cAcc<1> acc;
+        acc.zero();
         for (int64_t t = t_beg + warp; t < t_end; t += kTrackWarps)
-            tile_f32c<1>(tiles + t * (int64_t)kTileBytes, px, py, pz, bx, by, bz);
+            tile_f32c<1>(tiles + t * (int64_t)kTileBytes, ph, pl, acc);
+        bx[0] = acc.total(0, 0);
+        by[0] = acc.total(0, 1);
+        bz[0] = acc.total(0, 2);
     } else {
         for (int64_t t = t_beg + warp; t < t_end; t += kTrackWarps) {
             const int64_t a = s_beg + t * kTile, b = min(s_end, a + kTile);

@@ -70,9 +70,10 @@ int cct_field_f64(const double *d_kls, const double *d_p0s, int64_t n_seg,
                   void *stream);
 
 /* FP32-compensated form: segments re-packed once into tiles of
- * cct_f32c_tile() segments, each with an FP64 origin and FP32 offsets; the
- * sum runs in FP32 with Kahan-compensated tile partials and FP64 cross-tile
- * accumulation.  `packed` must be 256-byte aligned and hold
+ * cct_f32c_tile() segments, each with a double-float origin and FP32 offsets;
+ * point - origin is taken in double-float, the pair terms run in packed FP32,
+ * and the sum is Kahan-compensated in FP32 and resolved in FP64 (<= 1e-7
+ * relative inside the magnets).  `packed` must be 256-byte aligned and hold
  * cct_f32c_packed_bytes() bytes. */
 int64_t cct_f32c_packed_bytes(const int64_t *h_seg_off, int32_t n_designs);
 int cct_f32c_pack(const double *d_kls, const double *d_p0s,
@@ -121,9 +122,10 @@ int cct_track(const double *d_kls, const double *d_p0s, const int64_t *d_seg_off
               void *d_scratch, int64_t scratch_bytes, void *stream);
 
 /* Measures the device's fused multiply-add pipe peak (flop/s, 2 per FMA) with
- * independent FMA chains on every SM: fp64 = 0 for the FP32 pipe, 1 for FP64.
- * These are the roofline denominators of the field kernels.  Synchronous. */
-int cct_probe_fma_peak(int fp64, double *flops_per_s);
+ * independent FMA chains on every SM: kind 0 = scalar FP32, 1 = FP64, 2 = packed
+ * FP32x2.  These are the roofline denominators of the field kernels.
+ * Synchronous. */
+int cct_probe_fma_peak(int kind, double *flops_per_s);
 
 /* Test hook for failure detection without a GPU fault: makes every tracking
  * grid barrier expect `phantom_blocks` extra CTAs that never arrive, and sets

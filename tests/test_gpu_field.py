@@ -15,10 +15,18 @@ from tests.conftest import oracle_records
 
 F64_RTOL = 1e-12      # FP64 vs the reference FP64 CPU sum (norm-wise relative)
 F32C_RTOL = 1e-7      # FP32-compensated vs FP64 (the tolerance the FP32 form is built to)
+F32C_ATOL = 2e-8      # tesla: floor where layers of ~2.6 T cancel to tens of mT (fringe, drift)
 
 
 def rel(a, b):
     return np.linalg.norm(a - b, axis=-1) / np.linalg.norm(b, axis=-1)
+
+
+def f32c_ok(a, b):
+    """|dB| <= 1e-7 |B| + 2e-8 T at every point: relative inside the magnets (the field-map
+    tube points meet 1e-7 relative alone), absolute where layer fields of ~2.6 T cancel to
+    tens of millitesla (fringe and drift points, ~1.2e-8 T measured)."""
+    return bool(np.all(np.linalg.norm(a - b, axis=-1) <= F32C_RTOL * np.linalg.norm(b, axis=-1) + F32C_ATOL))
 
 
 @pytest.fixture(scope="module")
@@ -51,18 +59,16 @@ def test_single_point_api_matches_batch(golden, dipole):
     assert rel(np.array(b.to_list()), golden["sd_field_B"][3]) < F64_RTOL
 
 
-@pytest.mark.parametrize("prec,tol", [("f64", F64_RTOL), ("f32c", F32C_RTOL)])
-def test_hust2_beamline_with_qs(golden, prec, tol):
+def test_hust2_beamline_with_qs(golden):
     bl = HUST_SC_GANTRY().create_second_bending_part_beamline()     # 119 520 segments: ragged last tile
-    B = bl.magnetic_field_at_points(golden["h2_field_pts"], prec)
-    assert rel(B, golden["h2_field_B"]).max() < tol
+    assert rel(bl.magnetic_field_at_points(golden["h2_field_pts"], "f64"), golden["h2_field_B"]).max() < F64_RTOL
+    assert f32c_ok(bl.magnetic_field_at_points(golden["h2_field_pts"], "f32c"), golden["h2_field_B"])
 
 
-@pytest.mark.parametrize("prec,tol", [("f64", F64_RTOL), ("f32c", F32C_RTOL)])
-def test_gantry_section_vs_reference(golden, prec, tol):
+def test_gantry_section_vs_reference(golden):
     bl = W.build_gantry_section()
-    B = bl.magnetic_field_at_points(golden["gs_field_pts"], prec)
-    assert rel(B, golden["gs_field_B"]).max() < tol
+    assert rel(bl.magnetic_field_at_points(golden["gs_field_pts"], "f64"), golden["gs_field_B"]).max() < F64_RTOL
+    assert f32c_ok(bl.magnetic_field_at_points(golden["gs_field_pts"], "f32c"), golden["gs_field_B"])
 
 
 def test_qs_known_answer_bitwise(golden, records_json):
@@ -82,9 +88,8 @@ def test_qs_beamline_known_answer(golden, records_json):
     bl = (Beamline.set_start_point(P2()).first_drift(P2.x_direct(), 1)
           .append_qs(0.27, 5, 20, 100 * MM).append_drift(1)
           .append_dipole_cct(1, 100 * MM, 120 * MM, 45, [30], 60, 10000).append_drift(1))
-    for prec, tol in (("f64", F64_RTOL), ("f32c", F32C_RTOL)):
-        B = bl.magnetic_field_at_points(golden["qsbl_pts"], prec)
-        assert rel(B, golden["qsbl_B"]).max() < tol
+    assert rel(bl.magnetic_field_at_points(golden["qsbl_pts"], "f64"), golden["qsbl_B"]).max() < F64_RTOL
+    assert f32c_ok(bl.magnetic_field_at_points(golden["qsbl_pts"], "f32c"), golden["qsbl_B"])
     ga = GPU_ACCELERATOR(GPU_ACCELERATOR.FLOAT64)
     b = ga.magnet_at_beamline_with_single_qs(bl, P3(2.3, 50 * MM, 0)).to_list()
     # gpu_accelerator.py:1374 (printed by an earlier revision; ~5e-14 T away today)
@@ -153,7 +158,7 @@ def test_multi_design_packed_f32c(golden, dipole):
     b0 = engine.field_at_points(ds, golden["sd_field_pts"], "f32c", design=0)
     b1 = engine.field_at_points(ds, golden["h2_field_pts"], "f32c", design=1)
     assert rel(b0, golden["sd_field_B"]).max() < F32C_RTOL
-    assert rel(b1, golden["h2_field_B"]).max() < F32C_RTOL
+    assert f32c_ok(b1, golden["h2_field_B"])
 
 
 def test_torch_device_io(dipole):
