@@ -408,3 +408,173 @@ extern "C" int cct_test_set_barrier_fault(int phantom_blocks, int wait_ms) {
     cctgpu::g_wait_ms = wait_ms > 0 ? wait_ms : 60000;
     return CCT_OK;
 }
+
+// ============================================================================
+// Tracking without device allocation.
+//
+// Some callers cannot allocate device memory once they are running: a treatment-planning
+// or optimisation host that reserves its GPU memory at start-up and forbids cudaMalloc on
+// its hot path (an allocation there can fail mid-run or stall the device), or a plain C
+// caller that owns only the buffers it was handed.  cct_track_static_scratch gives them
+// the tracking kernel with its scratch in a fixed, file-scope device array instead of a
+// caller-provided buffer.  The array is created when the library is loaded, on every GPU
+// the process uses, and stays allocated until the process exits; its size bounds the
+// problem (see cctgpu.h).  All calls share it, so calls whose kernels overlap on the GPU
+// race on it; each call rewrites every word it reads before the kernel starts.
+// ============================================================================
+#include <mutex>
+
+namespace cctgpu {
+
+constexpr int64_t kStaticScratchBytes = 32LL << 20;   // 32 MiB
+constexpr int kStaticMaxDesigns = 64;
+constexpr int kStaticMaxDevices = 64;
+
+static __device__ __align__(256) unsigned char g_track_static_scratch[kStaticScratchBytes];
+static void *g_static_scratch_addr[kStaticMaxDevices];
+static std::mutex g_static_scratch_mutex;
+
+// Device address of the static scratch on the current device.  The first call on a
+// device looks the symbol up (cudaGetSymbolAddress) with that device current.
+static int static_scratch_address(void **out) {
+    int dev = 0;
+    CCT_TRY_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kStaticMaxDevices)
+        return set_error(CCT_ERR_UNSUPPORTED, "device ordinal %d beyond %d", dev, kStaticMaxDevices);
+    std::lock_guard<std::mutex> lock(g_static_scratch_mutex);
+    if (!g_static_scratch_addr[dev]) {
+        void *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_track_static_scratch);
+        if (e != cudaSuccess) return check_cuda(e, "cudaGetSymbolAddress(static tracking scratch)");
+        g_static_scratch_addr[dev] = p;
+    }
+    *out = g_static_scratch_addr[dev];
+    return CCT_OK;
+}
+
+static int launch_track_static(const double *kls, const double *p0s, const int64_t *seg_off, const void *packed,
+                               const double *qs, const int64_t *qs_off, int n_designs, double *particles,
+                               int64_t n_particles, double distance, double footstep, int precision,
+                               cudaStream_t st) {
+    if (n_designs > kStaticMaxDesigns)
+        return set_error(CCT_ERR_ARG, "%d designs exceed the %d the static-scratch entry point takes", n_designs,
+                         kStaticMaxDesigns);
+    void *scratch = nullptr;
+    int rc = static_scratch_address(&scratch);
+    if (rc != CCT_OK) return rc;
+
+    int64_t hoff[kStaticMaxDesigns + 1];
+    CCT_TRY_CUDA(cudaMemcpyAsync(hoff, seg_off, 8 * (n_designs + 1), cudaMemcpyDeviceToHost, st));
+    CCT_TRY_CUDA(cudaStreamSynchronize(st));
+    for (int d = 0; d < n_designs; ++d)
+        if (hoff[d + 1] < hoff[d]) return set_error(CCT_ERR_ARG, "segment offsets decrease at design %d", d);
+    const unsigned char *tiles = nullptr;
+    const int64_t *tile_off = nullptr;
+    if (precision == 1) {
+        int64_t ph[3];
+        CCT_TRY_CUDA(cudaMemcpyAsync(ph, packed, sizeof ph, cudaMemcpyDeviceToHost, st));
+        CCT_TRY_CUDA(cudaStreamSynchronize(st));
+        int64_t tiles_total = 0;
+        for (int d = 0; d < n_designs; ++d) tiles_total += (hoff[d + 1] - hoff[d] + kTile - 1) / kTile;
+        if (ph[0] != kPackedMagic || ph[1] != n_designs || ph[2] != tiles_total)
+            return set_error(CCT_ERR_ARG,
+                             "packed segments do not match the %d designs' segment offsets (built by "
+                             "cct_f32c_pack with the same offsets?)", n_designs);
+        tile_off = reinterpret_cast<const int64_t *>(static_cast<const unsigned char *>(packed) + kPackedHeaderBytes);
+        tiles = static_cast<const unsigned char *>(packed) + kPackedHeaderBytes + packed_index_bytes(n_designs);
+    }
+
+    int dev = 0, sms = 0, per_sm = 0, coop = 0;
+    CCT_TRY_CUDA(cudaGetDevice(&dev));
+    CCT_TRY_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    CCT_TRY_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
+    if (!coop) return set_error(CCT_ERR_UNSUPPORTED, "device %d has no cooperative launch", dev);
+    CCT_TRY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, track_kernel, kTrackBlock, 0));
+    if (per_sm < 1) return set_error(CCT_ERR_UNSUPPORTED, "tracking kernel does not fit on an SM");
+    const int grid = sms * per_sm;
+
+    const int64_t groups = (n_particles + 31) / 32;
+    int64_t tables[3 * kStaticMaxDesigns + 1];
+    int64_t *unit_off = tables, *chunks = unit_off + n_designs + 1, *chunk_tiles = chunks + n_designs;
+    const int64_t target = 8LL * grid;
+    int64_t want = (target + (int64_t)n_designs * groups - 1) / ((int64_t)n_designs * groups);
+    if (want < 1) want = 1;
+    if (want > kMaxChunks) want = kMaxChunks;
+    unit_off[0] = 0;
+    for (int d = 0; d < n_designs; ++d) {
+        const int64_t nt = (hoff[d + 1] - hoff[d] + kTile - 1) / kTile;
+        const int64_t ct = nt > 0 ? (nt + want - 1) / want : 1;
+        const int64_t cd = nt > 0 ? (nt + ct - 1) / ct : 1;
+        chunks[d] = cd;
+        chunk_tiles[d] = ct;
+        unit_off[d + 1] = unit_off[d] + groups * cd;
+    }
+    const TrackScratchLayout L = track_scratch_layout(n_designs, n_particles, unit_off[n_designs]);
+    if (L.total > kStaticScratchBytes)
+        return set_error(CCT_ERR_ARG,
+                         "%d designs x %lld particles need %lld bytes of tracking scratch; the static scratch holds "
+                         "%lld (use cct_track with a caller buffer)", n_designs, (long long)n_particles,
+                         (long long)L.total, (long long)kStaticScratchBytes);
+    unsigned char *sc = static_cast<unsigned char *>(scratch);
+    // the array keeps the previous call's contents: clear the control words, rewrite the tables
+    CCT_TRY_CUDA(cudaMemsetAsync(sc, 0, 256, st));
+    CCT_TRY_CUDA(cudaMemcpyAsync(sc + 256, tables, 8 * (3 * n_designs + 1), cudaMemcpyHostToDevice, st));
+
+    TrackParams P;
+    P.kls = kls;
+    P.p0s = p0s;
+    P.seg_off = seg_off;
+    P.tiles = tiles;
+    P.tile_off = tile_off;
+    P.qs = qs;
+    P.qs_off = qs_off;
+    P.n_designs = n_designs;
+    P.groups = (int)groups;
+    P.n_p = n_particles;
+    P.particles = particles;
+    P.distance = distance;
+    P.footstep = footstep;
+    P.state = reinterpret_cast<double *>(sc + L.state_off);
+    P.partial = reinterpret_cast<double *>(sc + L.partial_off);
+    P.ctrl = reinterpret_cast<unsigned *>(sc);
+    P.unit_off = reinterpret_cast<const int64_t *>(sc + 256);
+    P.chunks = P.unit_off + n_designs + 1;
+    P.chunk_tiles = P.chunks + n_designs;
+    P.precision = precision;
+    P.barrier_blocks = (unsigned)(grid + g_test_phantom_blocks);
+    P.wait_ns = (unsigned long long)g_wait_ms * 1000000ull;
+    void *args[] = {&P};
+    CCT_TRY_CUDA(cudaLaunchCooperativeKernel((const void *)track_kernel, dim3(grid), dim3(kTrackBlock), args, 0, st));
+
+    unsigned ctrl[8];
+    CCT_TRY_CUDA(cudaMemcpyAsync(ctrl, sc, sizeof ctrl, cudaMemcpyDeviceToHost, st));
+    CCT_TRY_CUDA(cudaStreamSynchronize(st));
+    if ((int)ctrl[CW_ERR] == CCT_ERR_TIMEOUT)
+        return set_error(CCT_ERR_TIMEOUT, "a tracking grid barrier waited longer than %lld ms", g_wait_ms);
+    if (ctrl[CW_NONFINITE])
+        return set_error(CCT_ERR_NONFINITE, "a particle state or step count was not finite");
+    return CCT_OK;
+}
+
+}  // namespace cctgpu
+
+extern "C" int64_t cct_track_static_scratch_bytes(void) { return cctgpu::kStaticScratchBytes; }
+
+extern "C" int cct_track_static_scratch(const double *d_kls, const double *d_p0s, const int64_t *d_seg_off,
+                                        const void *d_packed, const double *d_qs, const int64_t *d_qs_off,
+                                        int32_t n_designs, double *d_particles, int64_t n_particles, double distance,
+                                        double footstep, int32_t precision, void *stream) {
+    using namespace cctgpu;
+    clear_error();
+    if (n_designs <= 0 || n_particles < 0) return set_error(CCT_ERR_ARG, "need at least one design");
+    if (n_particles == 0) return CCT_OK;
+    if (!(distance > 0.0) || !(footstep > 0.0))
+        return set_error(CCT_ERR_ARG, "distance (%g) and footstep (%g) must be positive", distance, footstep);
+    if (precision != 0 && precision != 1) return set_error(CCT_ERR_ARG, "precision must be 0 or 1");
+    if (!d_seg_off || !d_qs_off || !d_particles) return set_error(CCT_ERR_ARG, "null pointer");
+    if (precision == 0 && (!d_kls || !d_p0s)) return set_error(CCT_ERR_ARG, "FP64 tracking needs segments");
+    if (precision == 1 && (!d_packed || reinterpret_cast<uintptr_t>(d_packed) % 256))
+        return set_error(CCT_ERR_ARG, "FP32c tracking needs a 256-byte aligned packed buffer");
+    return launch_track_static(d_kls, d_p0s, d_seg_off, d_packed, d_qs, d_qs_off, n_designs, d_particles,
+                               n_particles, distance, footstep, precision, static_cast<cudaStream_t>(stream));
+}

@@ -121,6 +121,29 @@ int cct_track(const double *d_kls, const double *d_p0s, const int64_t *d_seg_off
               double distance, double footstep, int32_t precision,
               void *d_scratch, int64_t scratch_bytes, void *stream);
 
+/* cct_track without any device allocation, for callers that may not allocate
+ * device memory once running (memory reserved up front by a host application;
+ * a C caller that owns only the buffers it passes).  No counterpart in the
+ * reference: cctpy's GPU path allocates and copies on every call.  The scratch
+ * is a fixed device array inside the library, created on each GPU when the
+ * library is loaded and held until the process exits; its size,
+ * cct_track_static_scratch_bytes() = 32 MiB, bounds the problem (for example
+ * 64 designs x 512 protons, or one design x 100 000 protons), and at most 64
+ * designs are taken.  Larger problems return CCT_ERR_ARG with the size they
+ * need; use cct_track with a caller buffer for them.  The first call on a
+ * device looks up the array's address on that device; make that first call
+ * before any stream capture.  Every call shares the array: calls whose kernels
+ * overlap on the GPU (other streams, other host threads) race and must be
+ * serialised by the caller.  Same arguments, results and status codes as
+ * cct_track otherwise; no cudaMalloc/cudaFree is made. */
+int64_t cct_track_static_scratch_bytes(void);
+int cct_track_static_scratch(const double *d_kls, const double *d_p0s,
+                             const int64_t *d_seg_off, const void *d_packed,
+                             const double *d_qs, const int64_t *d_qs_off,
+                             int32_t n_designs, double *d_particles,
+                             int64_t n_particles, double distance, double footstep,
+                             int32_t precision, void *stream);
+
 /* Measures the device's fused multiply-add pipe peak (flop/s, 2 per FMA) with
  * independent FMA chains on every SM: kind 0 = scalar FP32, 1 = FP64, 2 = packed
  * FP32x2.  These are the roofline denominators of the field kernels.
