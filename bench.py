@@ -139,6 +139,59 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+# ---------------------------------------------------------------- tracking (beside the headline)
+def measure_tracking(args, dev, rank):
+    """RK4 tracking throughput, FP32c vs FP64, on a slice of the tracking workloads:
+    the gantry section (597 600 segments, 4096 protons, 1 mm steps) and a design population
+    (64 second-section designs of uneven segment counts, 512 protons each, one launch).
+    Per-step cost does not depend on the track length, so a few steps stand for the 3.5 m
+    track.  Returns a dict of particle-steps/s and Gpairs/s."""
+    import torch
+    from cctpy_gb300 import HUST_SC_GANTRY, engine, workloads as W
+
+    def timed(ds, ps, steps, prec, reps=2):
+        engine.track(ds, ps, 0.002, 0.001, prec)          # warm-up (2 steps)
+        torch.cuda.synchronize()
+        best = float("inf")
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            engine.track(ds, ps, steps * 0.001, 0.001, prec)
+            torch.cuda.synchronize()
+            best = min(best, time.perf_counter() - t0)
+        return best
+
+    out = {}
+    bl = W.build_gantry_section()
+    ds = engine.design_of(bl)
+    ds.packed()
+    ps = W.beam_particles(bl, 4096, seed=2 + rank, kinetic_MeV=215.0)
+    n_seg = ds.n_segments
+    s32, s64 = args.track_steps, max(1, args.track_steps // 10)
+    t32 = timed(ds, ps, s32, "f32c")
+    t64 = timed(ds, ps, s64, "f64", reps=1)
+    r32, r64 = 4096 * s32 / t32, 4096 * s64 / t64
+    out["gantry_section"] = {
+        "workload": f"HUST second section, AG tilts [90,30,90,90], -7000 A, {n_seg} segments + 1 QS; 4096 protons "
+                    "215 MeV, 1 mm RK4 steps (one cooperative launch per call, host copies included)",
+        "f32c": {"steps": s32, "seconds": t32, "particle_steps_per_s": r32, "gpairs_per_s": r32 * 4 * n_seg / 1e9},
+        "f64": {"steps": s64, "seconds": t64, "particle_steps_per_s": r64, "gpairs_per_s": r64 * 4 * n_seg / 1e9},
+        "speedup_f32c_vs_f64": r32 / r64}
+    if not args.no_population:
+        bls = [HUST_SC_GANTRY(**kw).create_second_bending_part_beamline() for kw in W.design_population(64, seed=3)]
+        dsp = engine.design_set_of(bls)
+        dsp.packed()
+        pp = W.beam_particles(bls[0], 512, seed=2 + rank, kinetic_MeV=215.0)
+        tp = timed(dsp, pp, s32 // 2, "f32c", reps=1)
+        rp = 64 * 512 * (s32 // 2) / tp
+        segs = [dsp.segments_of(d) for d in range(64)]
+        out["design_population"] = {
+            "workload": f"64 designs ({min(segs)}..{max(segs)} segments, {dsp.n_segments} total), 512 protons each, "
+                        "one launch",
+            "f32c": {"steps": s32 // 2, "seconds": tp, "particle_steps_per_s": rp,
+                     "gpairs_per_s": 512 * (s32 // 2) * 4 * dsp.n_segments / tp / 1e9}}
+    return out
+
+
 # ---------------------------------------------------------------- GPU arm
 def run_ours(args):
     import torch
@@ -261,6 +314,8 @@ def run_ours(args):
         e2e_s = float(t)
     e2e = world * PAIRS * args.steps / e2e_s / 1e9
 
+    tracking = None if args.no_tracking else measure_tracking(args, dev, rank)
+
     line = None
     if rank == 0:
         cpu = None
@@ -296,6 +351,7 @@ def run_ours(args):
                                   "peak_source": "measured in this run: FP64 DFMA-chain probe"},
                      "speedup_f32c_vs_f64": value / f64_value},
             "accuracy": acc,
+            "tracking": tracking,
             "gpu_launches": args.steps,
             "clocks": clocks,
             "cpu_baseline": cpu,
@@ -316,6 +372,9 @@ def main():
     ap.add_argument("--cpu-points", type=int, default=16384)
     ap.add_argument("--ref-points", type=int, default=4096)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-tracking", action="store_true")
+    ap.add_argument("--no-population", action="store_true")
+    ap.add_argument("--track-steps", type=int, default=20, help="timed FP32c RK4 steps of the tracking slice")
     ap.add_argument("--traffic", type=float, default=None,
                     help="DRAM bytes per launch of the timed kernel from an ncu capture")
     args = ap.parse_args()

@@ -151,7 +151,7 @@ int64_t cct_track_scratch_bytes(int32_t n_designs, int64_t n_particles) {
         set_error(CCT_ERR_ARG, "need at least one design and one particle");
         return -1;
     }
-    return track_scratch_layout(n_designs, n_particles, track_max_units(n_designs, n_particles)).total;
+    return track_scratch_bound(n_designs, n_particles);
 }
 
 int cct_track(const double *d_kls, const double *d_p0s, const int64_t *d_seg_off, const void *d_packed,

@@ -45,8 +45,11 @@ int launch_field_f32c(const void *packed, int design, const double *qs, int n_qs
 struct TrackScratchLayout {
     int64_t state_off, partial_off, ctrl_off, total;
 };
-TrackScratchLayout track_scratch_layout(int n_designs, int64_t n_particles, int64_t n_units);
-int64_t track_max_units(int n_designs, int64_t n_particles);
+// Scratch layout for n_units units of `group` particles each.
+TrackScratchLayout track_scratch_layout(int n_designs, int64_t n_particles, int64_t n_units, int group);
+// Upper bound of the scratch any precision needs on the current device (or a generous
+// device-independent bound when no device is visible).
+int64_t track_scratch_bound(int n_designs, int64_t n_particles);
 int launch_track(const double *kls, const double *p0s, const int64_t *seg_off, const void *packed,
                  const double *qs, const int64_t *qs_off, int n_designs, double *particles, int64_t n_particles,
                  double distance, double footstep, int precision, void *scratch, int64_t scratch_bytes,

@@ -75,10 +75,12 @@ struct F32cAcc {
     __device__ __forceinline__ double total(int i, int c) const { return (double)S[i][c] - (double)C[i][c]; }
 };
 
-// Accumulate one tile for PPT points given as double-float (hi, lo) coordinates.
+// Accumulate segments [4*g0, 4*g1) of one tile (default: all 128) for PPT points given as
+// double-float (hi, lo) coordinates.
 template <int PPT>
 __device__ __forceinline__ void tile_f32c(const unsigned char *tile, const float (&ph)[PPT][3],
-                                          const float (&pl)[PPT][3], F32cAcc<PPT> &acc) {
+                                          const float (&pl)[PPT][3], F32cAcc<PPT> &acc, int g0 = 0,
+                                          int g1 = kTile / 4) {
     const TileHeader *h = reinterpret_cast<const TileHeader *>(tile);
     const ulonglong2 *v = reinterpret_cast<const ulonglong2 *>(tile + kTileHeaderBytes);
     constexpr int Q = kTile / 4;   // ulonglong2 (4 floats) per component array
@@ -91,12 +93,13 @@ __device__ __forceinline__ void tile_f32c(const unsigned char *tile, const float
             q[i][c] = f2_pack(d, d);
         }
 #pragma unroll 1
-    for (int sb = 0; sb < kTile / 64; ++sb) {
+    for (int sb = g0; sb < g1; sb += 16) {                       // sub-blocks of <= 64 segments
+        const int se = min(sb + 16, g1);
         f2 B[PPT][3];
 #pragma unroll
         for (int i = 0; i < PPT; ++i) B[i][0] = B[i][1] = B[i][2] = 0ull;
 #pragma unroll 1
-        for (int j = sb * 16; j < sb * 16 + 16; ++j) {          // 4 segments per iteration
+        for (int j = sb; j < se; ++j) {                          // 4 segments per iteration
             const ulonglong2 KX = v[0 * Q + j], KY = v[1 * Q + j], KZ = v[2 * Q + j];
             const ulonglong2 NX = v[3 * Q + j], NY = v[4 * Q + j], NZ = v[5 * Q + j];
             const ulonglong2 PX = v[6 * Q + j], PY = v[7 * Q + j], PZ = v[8 * Q + j];
