@@ -92,10 +92,12 @@ class Beamline(Line2, Magnet):
         length = big_r * abs(_rad(bending_angle))
         self.trajectory.add_arc_line(radius=big_r, clockwise=bending_angle < 0, angle_deg=abs(bending_angle))
         end_phi = _rad(bending_angle)
-        for small_r, tilts, ksi_end in ((small_r_inner, tilt_angles, 2 * math.pi * winding_number),
-                                        (small_r_outer, [t * -1 for t in tilt_angles], -2 * math.pi * winding_number)):
+        for role, small_r, tilts, ksi_end in (
+                ("dipole_inner", small_r_inner, tilt_angles, 2 * math.pi * winding_number),
+                ("dipole_outer", small_r_outer, [t * -1 for t in tilt_angles], -2 * math.pi * winding_number)):
             c = CCT.create_cct_along(self.trajectory, old, big_r, small_r, abs(bending_angle), tilts, winding_number,
                                      current, P2.origin(), P2(ksi_end, end_phi), disperse_number_per_winding)
+            c.role = role
             self.magnets.append(c)
             self.elements.append((old, c, length))
         return self._changed()
@@ -114,10 +116,11 @@ class Beamline(Line2, Magnet):
         length = big_r * abs(_rad(total))
         self.trajectory.add_arc_line(radius=big_r, clockwise=total < 0, angle_deg=abs(total))
         wd = winding_numbers[0][0]
-        for small_r, tilts, sign in ((small_rs[0], [t * -1 for t in tilt_angles[0]], -1),
-                                     (small_rs[1], tilt_angles[0], 1)):
+        for role, small_r, tilts, sign in (("dipole_outer", small_rs[0], [t * -1 for t in tilt_angles[0]], -1),
+                                           ("dipole_inner", small_rs[1], tilt_angles[0], 1)):
             c = CCT.create_cct_along(self.trajectory, old, big_r, small_r, abs(total), tilts, wd, currents[0],
                                      P2.origin(), P2(sign * 2 * math.pi * wd, _rad(total)), dpw)
+            c.role = role
             self.magnets.append(c)
             self.elements.append((old, c, length))
         ag_tilt, ag_cur, wn = tilt_angles[1], currents[1], winding_numbers[1]
@@ -133,10 +136,11 @@ class Beamline(Line2, Magnet):
             end_in = start_in + P2(sgn * 2 * math.pi * wn[k], rad[k])
             end_out = start_out + P2(-sgn * 2 * math.pi * wn[k], rad[k])
             part_len = big_r * _rad(abs(bending_angles[k]))
-            for small_r, tilts, a, b in ((small_rs[3], [t * -1 for t in ag_tilt], start_in, end_in),
-                                         (small_rs[2], ag_tilt, start_out, end_out)):
+            for role, small_r, tilts, a, b in (("ag_inner", small_rs[3], [t * -1 for t in ag_tilt], start_in, end_in),
+                                               ("ag_outer", small_rs[2], ag_tilt, start_out, end_out)):
                 c = CCT.create_cct_along(self.trajectory, old, big_r, small_r, abs(bending_angles[k]), tilts, wn[k],
                                          ag_cur, a, b, dpw)
+                c.role = role
                 self.magnets.append(c)
                 self.elements.append((s_part, c, part_len))
             s_part += part_len

@@ -1,0 +1,511 @@
+// Discrete adjoint of the batched RK4 track: gradient of a beam objective at the exit with
+// respect to every current element (kl, p0) of every design.
+//
+// Objective per design (over its N particles, positions p_i after the track, exit frame
+// (o, XI, YI) of the ideal particle): J = (1/N) sum_i (x_i^2 + y_i^2), x_i = XI.(p_i - o),
+// y_i = YI.(p_i - o) -- the RMS spot size squared plus the centroid squared in both planes.
+//
+// The adjoint is that of the exact discrete map the forward kernel applies (the reference's
+// RK4, base_utils.py:264-311, with f(Y) = [v, kq v x B(p)], particles.py:515-537), so it
+// agrees with finite differences of the forward up to their truncation error.  For one step,
+// with lambda' the adjoint after the step and J_f(Y)^T l = ((dB/dp)^T a, l_p + kq B x l_v),
+// a = kq (l_v x v):
+//   lk4 = h/6 l', mu4 = J_f(Y4)^T lk4;  lk3 = h/3 l' + h mu4,   mu3 = J_f(Y3)^T lk3;
+//   lk2 = h/3 l' + h/2 mu3, mu2 = ...;  lk1 = h/6 l' + h/2 mu2, mu1 = ...;
+//   l = l' + mu1 + mu2 + mu3 + mu4,
+// and every stage adds a . dB/d(segment) to the segment gradient:
+//   dJ/dkl_i += (r x a) / |r|^3,  dJ/dp0_i += -grad_p(a . B_i) = -(c/|r|^3 - 3 (c.r) r/|r|^5),
+//   r = p - p0_i, c = a x kl_i.
+//
+// Schedule (host, one stream, no synchronisation but the step count): initialise the state,
+// run the forward in segments of K steps keeping a checkpoint of the state before each,
+// evaluate J and dJ/dY at the exit, then for each checkpoint segment in reverse: restore,
+// re-run its K steps recording every stage's (Y, B), sweep its steps backwards
+// (adjoint_kernel: phase A' sums (dB/dp)^T a over segment chunks per particle block, as the
+// forward's phase A sums B; phase C' advances the lambdas), and accumulate the segment
+// gradient from the recorded (p, a) pairs (seg_adjoint_kernel, one thread per segment).
+// The adjoint sweeps run in FP64.
+#include <algorithm>
+#include <vector>
+
+#include "track_common.cuh"
+
+namespace cctgpu {
+
+constexpr int kAdjD = 24;   // per particle: LP (6), LY (6), LK (6), a (3), pad
+enum { AD_LP = 0, AD_LY = 6, AD_LK = 12, AD_A = 18 };
+
+struct AdjParams {
+    TrackParams T;              // the forward's parameters (plan, partials, state, record)
+    double *adj;                // per particle adjoint state
+    const double *exit_frame;   // per design: o (3), XI (3), YI (3)
+    double *J;                  // per design objective
+    int step_begin, step_end;   // the checkpoint segment swept here (in reverse)
+};
+
+// ---------------------------------------------------------------- objective and dJ/dY
+// One CTA per design: J_d and the adjoint of the final state (LY).
+__global__ void __launch_bounds__(256) objective_kernel(AdjParams A) {
+    const TrackParams &P = A.T;
+    const int d = blockIdx.x;
+    const double *f = A.exit_frame + 9 * d;
+    __shared__ double red[256];
+    double s = 0.0;
+    const double inv_n = 1.0 / (double)P.n_p;
+    for (int64_t j = threadIdx.x; j < P.n_p; j += blockDim.x) {
+        const int64_t pi = (int64_t)d * P.n_p + j;
+        const double *Y = P.state + pi * kStateD + ST_Y0;
+        const double dx = Y[0] - f[0], dy = Y[1] - f[1], dz = Y[2] - f[2];
+        const double x = f[3] * dx + f[4] * dy + f[5] * dz;
+        const double y = f[6] * dx + f[7] * dy + f[8] * dz;
+        s += x * x + y * y;
+        double *ad = A.adj + pi * kAdjD;
+        for (int c = 0; c < 3; ++c) {
+            ad[AD_LY + c] = 2.0 * inv_n * (x * f[3 + c] + y * f[6 + c]);
+            ad[AD_LY + 3 + c] = 0.0;
+        }
+    }
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {   // fixed-order tree: deterministic
+        if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) A.J[d] = red[0] * inv_n;
+}
+
+// ---------------------------------------------------------------- reverse sweep
+__device__ __forceinline__ double *rec_at(const TrackParams &P, int step, int stage, int64_t pi) {
+    return P.record + (((int64_t)(step - P.step_begin) * 4 + stage) * ((int64_t)P.n_designs * P.n_p) + pi) * kRec;
+}
+
+// Phase A': for the 32 particles of a unit's block, sum over the chunk's segments
+// grad_p (a . B_i) = c/|r|^3 - 3 (c.r) r / |r|^5, c = a x kl_i (FP64; G = 32, warps split tiles).
+__device__ void unit_grad_f64(const AdjParams &A, int64_t u, int step, int stage, TrackSmem &sm) {
+    const TrackParams &P = A.T;
+    const UnitRef U = locate_unit(P, u);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int64_t j = U.b * 32 + lane;
+    if (j >= P.n_p) j = P.n_p - 1;
+    const int64_t pi = (int64_t)U.d * P.n_p + j;
+    const double *rec = rec_at(P, step, stage, pi);
+    const double px = rec[0], py = rec[1], pz = rec[2];
+    const double *a = A.adj + pi * kAdjD + AD_A;
+    const double ax = a[0], ay = a[1], az = a[2];
+    double gx = 0.0, gy = 0.0, gz = 0.0;
+    const int64_t s_beg = P.seg_off[U.d], s_end = P.seg_off[U.d + 1];
+    for (int64_t t = U.t_beg + warp; t < U.t_end; t += kTrackWarps) {
+        const int64_t b0 = s_beg + t * kTile, e = min(s_end, b0 + kTile);
+        double tx = 0.0, ty = 0.0, tz = 0.0;
+        for (int64_t s = b0; s < e; ++s) {
+            const double kx = __ldg(P.kls + 3 * s), ky = __ldg(P.kls + 3 * s + 1), kz = __ldg(P.kls + 3 * s + 2);
+            const double rx = px - __ldg(P.p0s + 3 * s), ry = py - __ldg(P.p0s + 3 * s + 1),
+                         rz = pz - __ldg(P.p0s + 3 * s + 2);
+            const double inv = rsqrt(rx * rx + ry * ry + rz * rz);
+            const double inv3 = inv * inv * inv, inv5 = inv3 * inv * inv;
+            const double cx = ay * kz - az * ky, cy = az * kx - ax * kz, cz = ax * ky - ay * kx;
+            const double q = 3.0 * (cx * rx + cy * ry + cz * rz) * inv5;
+            tx += cx * inv3 - q * rx;
+            ty += cy * inv3 - q * ry;
+            tz += cz * inv3 - q * rz;
+        }
+        gx += tx;
+        gy += ty;
+        gz += tz;
+    }
+    double *red = sm.red + (warp * 32 + lane) * 3;
+    red[0] = gx;
+    red[1] = gy;
+    red[2] = gz;
+    __syncthreads();
+    if (warp == 0) {
+        double sx = 0.0, sy = 0.0, sz = 0.0;
+        for (int w = 0; w < kTrackWarps; ++w) {
+            const double *r = sm.red + (w * 32 + lane) * 3;
+            sx += r[0];
+            sy += r[1];
+            sz += r[2];
+        }
+        double *out = P.partial + (u * 32 + lane) * 3;
+        out[0] = sx;
+        out[1] = sy;
+        out[2] = sz;
+    }
+    __syncthreads();
+}
+
+// grad_p (a . B_qs) of one QS magnet (magnets.py:637-668: bx = g y + s x y,
+// by = g x + s (x^2 - y^2) / 2 in the local frame, zero outside); added to g.
+__device__ __forceinline__ void qs_grad_add(const double *q, const double *p, const double *a, double *g) {
+    const double dx = p[0] - q[0], dy = p[1] - q[1], dz = p[2] - q[2];
+    const double x = q[3] * dx + q[4] * dy + q[5] * dz;
+    const double y = q[6] * dx + q[7] * dy + q[8] * dz;
+    const double z = q[9] * dx + q[10] * dy + q[11] * dz;
+    if (z < 0.0 || z > q[12]) return;
+    const double ap = q[15];
+    if (fabs(x) > ap || fabs(y) > ap || sqrt(x * x + y * y) > ap) return;
+    const double gr = q[13], s = q[14];
+    const double al = a[0] * q[3] + a[1] * q[4] + a[2] * q[5];   // a . XI
+    const double be = a[0] * q[6] + a[1] * q[7] + a[2] * q[8];   // a . YI
+    const double dfx = al * s * y + be * (gr + s * x);            // d(a.B)/dx
+    const double dfy = al * (gr + s * x) - be * s * y;            // d(a.B)/dy
+    for (int c = 0; c < 3; ++c) g[c] += q[3 + c] * dfx + q[6 + c] * dfy;
+}
+
+// a = kq (l_v x v) for the stage `stage` (0-based) of `step`; written to the particle's
+// adjoint state and to the record (for the segment gradient).
+__device__ __forceinline__ void set_weight(const AdjParams &A, int64_t pi, int step, int stage, const double *lk) {
+    const TrackParams &P = A.T;
+    double *rec = rec_at(P, step, stage, pi);
+    const double kq = P.state[pi * kStateD + ST_KQ];
+    const double *v = rec + 3;
+    double *a = A.adj + pi * kAdjD + AD_A;
+    a[0] = kq * (lk[4] * v[2] - lk[5] * v[1]);
+    a[1] = kq * (lk[5] * v[0] - lk[3] * v[2]);
+    a[2] = kq * (lk[3] * v[1] - lk[4] * v[0]);
+    rec[9] = a[0];
+    rec[10] = a[1];
+    rec[11] = a[2];
+}
+
+__device__ __forceinline__ void clear_weight(const AdjParams &A, int64_t pi, int step, int stage) {
+    double *rec = rec_at(A.T, step, stage, pi);
+    double *a = A.adj + pi * kAdjD + AD_A;
+    a[0] = a[1] = a[2] = rec[9] = rec[10] = rec[11] = 0.0;
+}
+
+// Start of a step in reverse: l' = LY, lk4 = h/6 l', weight of stage 4.
+__device__ void begin_step(const AdjParams &A, int64_t pi, int step) {
+    const TrackParams &P = A.T;
+    const double *S = P.state + pi * kStateD;
+    if ((double)step >= S[ST_NSTEPS]) {
+        for (int s = 0; s < 4; ++s) clear_weight(A, pi, step, s);
+        return;
+    }
+    double *ad = A.adj + pi * kAdjD;
+    const double h = S[ST_DT];
+    for (int c = 0; c < 6; ++c) {
+        ad[AD_LP + c] = ad[AD_LY + c];
+        ad[AD_LK + c] = h / 6 * ad[AD_LP + c];
+    }
+    set_weight(A, pi, step, 3, ad + AD_LK);
+}
+
+// Phase C' of stage `stage` (3..0): mu = J_f^T lk, LY += mu, next lk and weight.
+__device__ void end_stage(const AdjParams &A, int64_t pi, int step, int stage) {
+    const TrackParams &P = A.T;
+    const double *S = P.state + pi * kStateD;
+    if ((double)step >= S[ST_NSTEPS]) return;
+    const int d = (int)(pi / P.n_p);
+    const int64_t j = pi % P.n_p, b = j / P.G, slot = j % P.G;
+    const int64_t cd = P.chunks[d], u0 = P.unit_off[d] + b * cd;
+    double mu[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    for (int64_t c = 0; c < cd; ++c) {
+        const double *p = P.partial + ((u0 + c) * P.G + slot) * 3;
+        mu[0] += p[0];
+        mu[1] += p[1];
+        mu[2] += p[2];
+    }
+    const double *rec = rec_at(P, step, stage, pi);
+    double *ad = A.adj + pi * kAdjD;
+    for (int64_t q = P.qs_off[d]; q < P.qs_off[d + 1]; ++q) qs_grad_add(P.qs + kQsRecord * q, rec, ad + AD_A, mu);
+    const double kq = S[ST_KQ];
+    const double *B = rec + 6, *lk = ad + AD_LK;
+    mu[3] = lk[0] + kq * (B[1] * lk[5] - B[2] * lk[4]);
+    mu[4] = lk[1] + kq * (B[2] * lk[3] - B[0] * lk[5]);
+    mu[5] = lk[2] + kq * (B[0] * lk[4] - B[1] * lk[3]);
+    for (int c = 0; c < 6; ++c) ad[AD_LY + c] += mu[c];
+    if (stage > 0) {
+        const double h = S[ST_DT];
+        const double cl = stage == 1 ? h / 6 : h / 3;    // coefficient of l' in lk(stage-1)
+        const double cm = stage == 3 ? h : h / 2;        // coefficient of mu in lk(stage-1)
+        double nk[6];
+        for (int c = 0; c < 6; ++c) nk[c] = cl * ad[AD_LP + c] + cm * mu[c];
+        for (int c = 0; c < 6; ++c) ad[AD_LK + c] = nk[c];
+        set_weight(A, pi, step, stage - 1, nk);
+    }
+}
+
+__global__ void __launch_bounds__(kTrackBlock) adjoint_kernel(AdjParams A) {
+    __shared__ __align__(128) TrackSmem sm;
+    const TrackParams &P = A.T;
+    const int64_t total = (int64_t)P.n_designs * P.n_p;
+    const int64_t tstride = (int64_t)gridDim.x * blockDim.x;
+    const int64_t n_units = P.unit_off[P.n_designs];
+    const int64_t first = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (A.step_end <= A.step_begin) return;
+    for (int64_t pi = first; pi < total; pi += tstride) begin_step(A, pi, A.step_end - 1);
+    if (!grid_barrier(P, sm)) return;
+    for (int step = A.step_end - 1; step >= A.step_begin; --step) {
+        for (int stage = 3; stage >= 0; --stage) {
+            for (int64_t u = blockIdx.x; u < n_units; u += gridDim.x) unit_grad_f64(A, u, step, stage, sm);
+            if (!grid_barrier(P, sm)) return;
+            for (int64_t pi = first; pi < total; pi += tstride) {
+                end_stage(A, pi, step, stage);
+                if (stage == 0 && step > A.step_begin) begin_step(A, pi, step - 1);
+            }
+            if (!grid_barrier(P, sm)) return;
+        }
+    }
+}
+
+// ---------------------------------------------------------------- segment gradient
+// One thread per segment of design blockIdx.y; the design's recorded (p, a) pairs of the
+// segment of steps stream through shared memory.  Adds into grad[seg][6] (dJ/dkl, dJ/dp0).
+constexpr int kSegBlock = 256;
+
+__global__ void __launch_bounds__(kSegBlock) seg_adjoint_kernel(TrackParams P, int n_steps, double *grad) {
+    __shared__ double pts[kSegBlock][6];
+    const int d = blockIdx.y;
+    const int64_t s_beg = P.seg_off[d], s_end = P.seg_off[d + 1];
+    const int64_t s = s_beg + (int64_t)blockIdx.x * kSegBlock + threadIdx.x;
+    if (s_beg + (int64_t)blockIdx.x * kSegBlock >= s_end) return;   // whole CTA beyond this design
+    const bool mine = s < s_end;
+    double kx = 0, ky = 0, kz = 0, qx = 0, qy = 0, qz = 0;
+    if (mine) {
+        kx = P.kls[3 * s];
+        ky = P.kls[3 * s + 1];
+        kz = P.kls[3 * s + 2];
+        qx = P.p0s[3 * s];
+        qy = P.p0s[3 * s + 1];
+        qz = P.p0s[3 * s + 2];
+    }
+    double gk[3] = {0, 0, 0}, gp[3] = {0, 0, 0};
+    const int64_t total = (int64_t)P.n_designs * P.n_p;
+    const int64_t n_pts = (int64_t)n_steps * 4 * P.n_p;   // this design's (step, stage, particle)
+    for (int64_t base = 0; base < n_pts; base += kSegBlock) {
+        __syncthreads();
+        const int64_t e = base + threadIdx.x;
+        if (e < n_pts) {
+            const int64_t ss = e / P.n_p, j = e % P.n_p;
+            const double *r = P.record + (ss * total + (int64_t)d * P.n_p + j) * kRec;
+            pts[threadIdx.x][0] = r[0];
+            pts[threadIdx.x][1] = r[1];
+            pts[threadIdx.x][2] = r[2];
+            pts[threadIdx.x][3] = r[9];
+            pts[threadIdx.x][4] = r[10];
+            pts[threadIdx.x][5] = r[11];
+        } else {
+            for (int c = 0; c < 6; ++c) pts[threadIdx.x][c] = 0.0;
+        }
+        __syncthreads();
+        const int cnt = (int)min((int64_t)kSegBlock, n_pts - base);
+        double tk[3] = {0, 0, 0}, tp[3] = {0, 0, 0};
+        for (int i = 0; i < cnt; ++i) {
+            const double ax = pts[i][3], ay = pts[i][4], az = pts[i][5];
+            if (ax == 0.0 && ay == 0.0 && az == 0.0) continue;      // inactive stage (uniform)
+            const double rx = pts[i][0] - qx, ry = pts[i][1] - qy, rz = pts[i][2] - qz;
+            const double inv = rsqrt(rx * rx + ry * ry + rz * rz);
+            const double inv3 = inv * inv * inv, inv5 = inv3 * inv * inv;
+            tk[0] += (ry * az - rz * ay) * inv3;
+            tk[1] += (rz * ax - rx * az) * inv3;
+            tk[2] += (rx * ay - ry * ax) * inv3;
+            const double cx = ay * kz - az * ky, cy = az * kx - ax * kz, cz = ax * ky - ay * kx;
+            const double q = 3.0 * (cx * rx + cy * ry + cz * rz) * inv5;
+            tp[0] -= cx * inv3 - q * rx;
+            tp[1] -= cy * inv3 - q * ry;
+            tp[2] -= cz * inv3 - q * rz;
+        }
+        for (int c = 0; c < 3; ++c) {
+            gk[c] += tk[c];
+            gp[c] += tp[c];
+        }
+    }
+    if (mine) {
+        for (int c = 0; c < 3; ++c) {
+            grad[6 * s + c] += gk[c];
+            grad[6 * s + 3 + c] += gp[c];
+        }
+    }
+}
+
+// ---------------------------------------------------------------- host side
+struct AdjLayout {
+    int64_t track_total, ckpt_off, record_off, adj_off, total;
+};
+
+static AdjLayout adj_layout(const TrackScratchLayout &L, int n_designs, int64_t n_p, int n_ckpt, int K) {
+    auto up = [](int64_t b) { return (b + 255) / 256 * 256; };
+    const int64_t tot = (int64_t)n_designs * n_p;
+    AdjLayout A;
+    A.track_total = L.total;
+    A.ckpt_off = up(L.total);
+    A.record_off = A.ckpt_off + up(8 * kStateD * tot * (int64_t)n_ckpt);
+    A.adj_off = A.record_off + up(8 * (int64_t)kRec * 4 * K * tot);
+    A.total = A.adj_off + up(8 * kAdjD * tot);
+    return A;
+}
+
+static int adjoint_grid(int *grid_out) {
+    int dev = 0, sms = 0, per_sm = 0;
+    CCT_TRY_CUDA(cudaGetDevice(&dev));
+    CCT_TRY_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    CCT_TRY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, adjoint_kernel, kTrackBlock, 0));
+    if (per_sm < 1) return set_error(CCT_ERR_UNSUPPORTED, "adjoint kernel does not fit on an SM");
+    *grid_out = sms * per_sm;
+    return CCT_OK;
+}
+
+static int64_t adjoint_scratch_bound(int n_designs, int64_t n_p, int max_steps, int K) {
+    const int64_t track = track_scratch_bound(n_designs, n_p);
+    TrackScratchLayout L{0, 0, 0, track};
+    const int n_ckpt = (max_steps + K - 1) / K;
+    return adj_layout(L, n_designs, n_p, n_ckpt, K).total;
+}
+
+static int launch_adjoint(const double *kls, const double *p0s, const int64_t *seg_off, const double *qs,
+                   const int64_t *qs_off, int n_designs, double *particles, int64_t n_p, double distance,
+                   double footstep, const double *exit_frame, double *J, double *seg_grad, int K, void *scratch,
+                   int64_t scratch_bytes, cudaStream_t st) {
+    std::vector<int64_t> hoff(n_designs + 1), tables(3 * n_designs + 1);
+    CCT_TRY_CUDA(cudaMemcpyAsync(hoff.data(), seg_off, 8 * (n_designs + 1), cudaMemcpyDeviceToHost, st));
+    CCT_TRY_CUDA(cudaStreamSynchronize(st));
+    for (int d = 0; d < n_designs; ++d)
+        if (hoff[d + 1] < hoff[d]) return set_error(CCT_ERR_ARG, "segment offsets decrease at design %d", d);
+    int grid = 0, agrid = 0;
+    int rc = track_grid(&grid);
+    if (rc == CCT_OK) rc = adjoint_grid(&agrid);
+    if (rc != CCT_OK) return rc;
+    const int G = group_size(0, n_p);
+    int64_t *unit_off = tables.data(), *chunks = unit_off + n_designs + 1, *chunk_tiles = chunks + n_designs;
+    const int64_t n_units = plan_units(hoff.data(), n_designs, n_p, G, grid, unit_off, chunks, chunk_tiles);
+    const TrackScratchLayout L = track_scratch_layout(n_designs, n_p, n_units, G);
+    if (reinterpret_cast<uintptr_t>(scratch) % 256) return set_error(CCT_ERR_ARG, "adjoint scratch must be 256-byte aligned");
+    if (scratch_bytes < L.total) return set_error(CCT_ERR_ARG, "adjoint scratch too small (%lld bytes)", (long long)scratch_bytes);
+    unsigned char *sc = static_cast<unsigned char *>(scratch);
+    const int64_t tot = (int64_t)n_designs * n_p;
+
+    TrackParams P;
+    P.kls = kls;
+    P.p0s = p0s;
+    P.seg_off = seg_off;
+    P.tiles = nullptr;
+    P.tile_off = nullptr;
+    P.qs = qs;
+    P.qs_off = qs_off;
+    P.n_designs = n_designs;
+    P.G = G;
+    P.ppt = 1;
+    P.n_p = n_p;
+    P.particles = particles;
+    P.distance = distance;
+    P.footstep = footstep;
+    P.state = reinterpret_cast<double *>(sc + L.state_off);
+    P.partial = reinterpret_cast<double *>(sc + L.partial_off);
+    P.ctrl = reinterpret_cast<unsigned *>(sc);
+    P.unit_off = reinterpret_cast<const int64_t *>(sc + 256);
+    P.chunks = P.unit_off + n_designs + 1;
+    P.chunk_tiles = P.chunks + n_designs;
+    P.precision = 0;
+    P.barrier_blocks = (unsigned)(grid + g_test_phantom_blocks);
+    P.wait_ns = (unsigned long long)g_wait_ms * 1000000ull;
+    P.record = nullptr;
+
+    // 1. state from the records; learn the step count
+    CCT_TRY_CUDA(cudaMemsetAsync(sc, 0, 256, st));
+    CCT_TRY_CUDA(cudaMemcpyAsync(sc + 256, tables.data(), 8 * tables.size(), cudaMemcpyHostToDevice, st));
+    P.init_from_records = 1;
+    P.write_back = 0;
+    P.step_begin = 0;
+    P.step_end = 0;
+    CCT_TRY_CUDA(launch_track_kernel(P, grid, st));
+    unsigned ctrl[8];
+    CCT_TRY_CUDA(cudaMemcpyAsync(ctrl, sc, sizeof ctrl, cudaMemcpyDeviceToHost, st));
+    CCT_TRY_CUDA(cudaStreamSynchronize(st));
+    if ((int)ctrl[CW_ERR] == CCT_ERR_TIMEOUT) return set_error(CCT_ERR_TIMEOUT, "adjoint: initialisation timed out");
+    if (ctrl[CW_NONFINITE]) return set_error(CCT_ERR_NONFINITE, "adjoint: a particle step count was not finite");
+    const int steps = (int)ctrl[CW_MAXSTEPS];
+    if (K < 1) K = 64;
+    const int n_ckpt = (steps + K - 1) / K;
+    const AdjLayout AL = adj_layout(L, n_designs, n_p, n_ckpt, K);
+    if (scratch_bytes < AL.total)
+        return set_error(CCT_ERR_ARG, "adjoint needs %lld bytes of scratch for %d steps (K = %d), %lld given",
+                         (long long)AL.total, steps, K, (long long)scratch_bytes);
+    double *ckpt = reinterpret_cast<double *>(sc + AL.ckpt_off);
+    double *record = reinterpret_cast<double *>(sc + AL.record_off);
+    const size_t state_bytes = 8 * (size_t)kStateD * tot;
+
+    // 2. forward in checkpoint segments
+    P.init_from_records = 0;
+    for (int c = 0; c < n_ckpt; ++c) {
+        CCT_TRY_CUDA(cudaMemcpyAsync(ckpt + (int64_t)c * kStateD * tot, P.state, state_bytes, cudaMemcpyDeviceToDevice,
+                                     st));
+        P.step_begin = c * K;
+        P.step_end = std::min(steps, (c + 1) * K);
+        P.write_back = c == n_ckpt - 1;
+        CCT_TRY_CUDA(launch_track_kernel(P, grid, st));
+    }
+
+    // 3. objective and the adjoint of the final state
+    AdjParams A;
+    A.T = P;
+    A.adj = reinterpret_cast<double *>(sc + AL.adj_off);
+    A.exit_frame = exit_frame;
+    A.J = J;
+    objective_kernel<<<n_designs, 256, 0, st>>>(A);
+    CCT_TRY_CUDA(cudaGetLastError());
+    CCT_TRY_CUDA(cudaMemsetAsync(seg_grad, 0, 48 * (size_t)hoff[n_designs], st));
+
+    // 4. reverse over the checkpoint segments
+    int64_t max_seg = 0;
+    for (int d = 0; d < n_designs; ++d) max_seg = std::max(max_seg, hoff[d + 1] - hoff[d]);
+    for (int c = n_ckpt - 1; c >= 0; --c) {
+        CCT_TRY_CUDA(cudaMemcpyAsync(P.state, ckpt + (int64_t)c * kStateD * tot, state_bytes, cudaMemcpyDeviceToDevice,
+                                     st));
+        P.step_begin = c * K;
+        P.step_end = std::min(steps, (c + 1) * K);
+        P.write_back = 0;
+        P.record = record;
+        CCT_TRY_CUDA(launch_track_kernel(P, grid, st));
+        A.T = P;
+        A.T.barrier_blocks = (unsigned)(agrid + g_test_phantom_blocks);
+        A.step_begin = P.step_begin;
+        A.step_end = P.step_end;
+        void *args[] = {&A};
+        CCT_TRY_CUDA(cudaLaunchCooperativeKernel((const void *)adjoint_kernel, dim3(agrid), dim3(kTrackBlock), args,
+                                                 0, st));
+        if (max_seg > 0) {
+            const dim3 sg((unsigned)((max_seg + kSegBlock - 1) / kSegBlock), (unsigned)n_designs);
+            seg_adjoint_kernel<<<sg, kSegBlock, 0, st>>>(P, P.step_end - P.step_begin, seg_grad);
+            CCT_TRY_CUDA(cudaGetLastError());
+        }
+        P.record = nullptr;
+    }
+    CCT_TRY_CUDA(cudaMemcpyAsync(ctrl, sc, sizeof ctrl, cudaMemcpyDeviceToHost, st));
+    CCT_TRY_CUDA(cudaStreamSynchronize(st));
+    if ((int)ctrl[CW_ERR] == CCT_ERR_TIMEOUT)
+        return set_error(CCT_ERR_TIMEOUT, "adjoint: a grid barrier or tile copy waited longer than its limit");
+    if (ctrl[CW_NONFINITE]) return set_error(CCT_ERR_NONFINITE, "adjoint: a particle state was not finite");
+    return CCT_OK;
+}
+
+}  // namespace cctgpu
+
+extern "C" int64_t cct_adjoint_scratch_bytes(int32_t n_designs, int64_t n_particles, int32_t max_steps,
+                                             int32_t checkpoint_steps) {
+    using namespace cctgpu;
+    clear_error();
+    if (n_designs <= 0 || n_particles <= 0 || max_steps <= 0) {
+        set_error(CCT_ERR_ARG, "need at least one design, one particle and one step");
+        return -1;
+    }
+    return adjoint_scratch_bound(n_designs, n_particles, max_steps, checkpoint_steps > 0 ? checkpoint_steps : 64);
+}
+
+extern "C" int cct_track_adjoint(const double *d_kls, const double *d_p0s, const int64_t *d_seg_off,
+                                 const double *d_qs, const int64_t *d_qs_off, int32_t n_designs, double *d_particles,
+                                 int64_t n_particles, double distance, double footstep, const double *d_exit_frame,
+                                 double *d_J, double *d_seg_grad, int32_t checkpoint_steps, void *d_scratch,
+                                 int64_t scratch_bytes, void *stream) {
+    using namespace cctgpu;
+    clear_error();
+    if (n_designs <= 0 || n_particles <= 0) return set_error(CCT_ERR_ARG, "need at least one design and particle");
+    if (!(distance > 0.0) || !(footstep > 0.0))
+        return set_error(CCT_ERR_ARG, "distance (%g) and footstep (%g) must be positive", distance, footstep);
+    if (!d_kls || !d_p0s || !d_seg_off || !d_qs_off || !d_particles || !d_exit_frame || !d_J || !d_seg_grad ||
+        !d_scratch)
+        return set_error(CCT_ERR_ARG, "null pointer");
+    return launch_adjoint(d_kls, d_p0s, d_seg_off, d_qs, d_qs_off, n_designs, d_particles, n_particles, distance,
+                          footstep, d_exit_frame, d_J, d_seg_grad, checkpoint_steps, d_scratch, scratch_bytes,
+                          static_cast<cudaStream_t>(stream));
+}

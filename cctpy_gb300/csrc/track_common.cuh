@@ -1,0 +1,351 @@
+// Device-side pieces of the tracking kernels shared by track.cu (forward RK4) and
+// adjoint.cu (checkpointed reverse sweep): parameters, shared memory, bounded grid barrier,
+// unit decomposition, the phase-A field sums and the phase-C RK4 bookkeeping.
+#pragma once
+
+#include "cctgpu_internal.cuh"
+#include "qs.cuh"
+#include "tile.cuh"
+
+namespace cctgpu {
+
+constexpr int kTrackBlock = 256;
+constexpr int kTrackWarps = kTrackBlock / 32;
+constexpr int kStateD = 24;          // doubles of RK4 state per particle
+constexpr int kMaxChunks = 4096;     // chunks per (design, block)
+constexpr int kUnitsPerCta = 4;      // target units per CTA and stage (load balance)
+constexpr int kRing = 4;             // TMA ring depth (tiles)
+constexpr int kRedDoubles = 512 * 3; // per-CTA reduction buffer: S slices x G particles x 3
+constexpr uint32_t kTmaPolls = 1u << 22;
+
+// control words
+enum { CW_COUNT = 0, CW_GEN = 1, CW_ERR = 2, CW_NONFINITE = 3, CW_MAXSTEPS = 4 };
+
+// state layout per particle
+enum { ST_Y0 = 0, ST_YS = 6, ST_KSUM = 12, ST_DT = 18, ST_KQ = 19, ST_NSTEPS = 20 };
+
+struct TrackParams {
+    const double *kls, *p0s;
+    const int64_t *seg_off;
+    const unsigned char *tiles;    // FP32c tiles base (precision 1)
+    const int64_t *tile_off;       // FP32c per-design first tile (precision 1)
+    const double *qs;
+    const int64_t *qs_off;
+    int n_designs;
+    int G;                         // particles per unit
+    int ppt;                       // particles per lane in FP32c phase A (1 or 2)
+    int64_t n_p;
+    double *particles;
+    double distance, footstep;
+    double *state, *partial;
+    unsigned *ctrl;
+    const int64_t *unit_off;       // [n_designs+1] first unit of each design
+    const int64_t *chunks;         // [n_designs] chunks per block
+    const int64_t *chunk_tiles;    // [n_designs] tiles per chunk
+    int precision;
+    unsigned barrier_blocks;       // CTAs expected at each barrier
+    unsigned long long wait_ns;    // barrier wait limit
+    // step range and I/O of one launch (the adjoint runs the track in checkpoint segments)
+    int init_from_records;         // 1: state from the particle records (and step count)
+    int write_back;                // 1: write the final state into the particle records
+    int step_begin, step_end;      // steps [step_begin, min(step_end, step count)) run here
+    double *record;                // null, or per (step, stage, particle): stage state + field
+};
+
+// record entry of one (step, stage, particle): stage Y (6), B at the stage position (3),
+// adjoint weight a = kq (lambda_v x v) written by the reverse sweep (3)
+constexpr int kRec = 12;
+
+struct TrackSmem {
+    unsigned char ring[kRing][kTileBytes];
+    uint64_t full[kRing];
+    double red[kRedDoubles];
+    int verdict;
+};
+
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ void set_timeout(const TrackParams &P) {
+    atomicCAS(reinterpret_cast<int *>(P.ctrl + CW_ERR), 0, (int)CCT_ERR_TIMEOUT);
+}
+
+// Grid-wide barrier with a wall-clock limit; every thread of the CTA returns the same
+// verdict (false = some CTA timed out, stop).
+static __device__ bool grid_barrier(const TrackParams &P, TrackSmem &sm) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile unsigned *gen = P.ctrl + CW_GEN;
+        volatile int *err = reinterpret_cast<volatile int *>(P.ctrl + CW_ERR);
+        const unsigned g = *gen;
+        __threadfence();
+        const unsigned prev = atomicAdd(P.ctrl + CW_COUNT, 1u);
+        if (prev == P.barrier_blocks - 1) {
+            atomicExch(P.ctrl + CW_COUNT, 0u);
+            __threadfence();
+            atomicAdd(P.ctrl + CW_GEN, 1u);
+        } else {
+            const unsigned long long t0 = global_ns();
+            unsigned polls = 0;
+            while (*gen == g) {
+                if (*err == CCT_ERR_TIMEOUT) break;
+                if ((++polls & 255u) == 0 && global_ns() - t0 > P.wait_ns) {
+                    set_timeout(P);
+                    break;
+                }
+                __nanosleep(128);
+            }
+        }
+        __threadfence();
+        sm.verdict = (*err == CCT_ERR_TIMEOUT) ? 0 : 1;
+    }
+    __syncthreads();
+    return sm.verdict != 0;
+}
+
+// cross product with the reference's component formula (point.py:402-410), unfused
+__device__ __forceinline__ void cross_rn(double ax, double ay, double az, double bx, double by, double bz,
+                                         double &cx, double &cy, double &cz) {
+    cx = __dadd_rn(__dmul_rn(ay, bz), -__dmul_rn(az, by));
+    cy = __dadd_rn(-__dmul_rn(ax, bz), __dmul_rn(az, bx));
+    cz = __dadd_rn(__dmul_rn(ax, by), -__dmul_rn(ay, bx));
+}
+
+struct UnitRef {
+    int d;
+    int64_t b, c, t_beg, t_end;
+};
+
+__device__ __forceinline__ UnitRef locate_unit(const TrackParams &P, int64_t u) {
+    int lo = 0, hi = P.n_designs - 1;   // last d with unit_off[d] <= u
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) / 2;
+        if (P.unit_off[mid] <= u) lo = mid; else hi = mid - 1;
+    }
+    UnitRef r;
+    r.d = lo;
+    const int64_t cd = P.chunks[lo], local = u - P.unit_off[lo];
+    r.b = local / cd;
+    r.c = local % cd;
+    const int64_t nt = (P.seg_off[lo + 1] - P.seg_off[lo] + kTile - 1) / kTile;
+    const int64_t ct = P.chunk_tiles[lo];
+    r.t_beg = r.c * ct;
+    r.t_end = min(nt, (r.c + 1) * ct);
+    return r;
+}
+
+// Phase A, FP64: G = 32, warps split the chunk's tiles, lane = particle.
+static __device__ void unit_field_f64(const TrackParams &P, int64_t u, TrackSmem &sm) {
+    const UnitRef U = locate_unit(P, u);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int64_t j = U.b * 32 + lane;
+    if (j >= P.n_p) j = P.n_p - 1;
+    const double *Ys = P.state + ((int64_t)U.d * P.n_p + j) * kStateD + ST_YS;
+    const double px = Ys[0], py = Ys[1], pz = Ys[2];
+    double bx = 0.0, by = 0.0, bz = 0.0;
+    const int64_t s_beg = P.seg_off[U.d], s_end = P.seg_off[U.d + 1];
+    for (int64_t t = U.t_beg + warp; t < U.t_end; t += kTrackWarps) {
+        const int64_t a = s_beg + t * kTile, e = min(s_end, a + kTile);
+        double tx = 0.0, ty = 0.0, tz = 0.0;
+        for (int64_t s = a; s < e; ++s) {
+            const double kx = __ldg(P.kls + 3 * s), ky = __ldg(P.kls + 3 * s + 1), kz = __ldg(P.kls + 3 * s + 2);
+            const double rx = px - __ldg(P.p0s + 3 * s), ry = py - __ldg(P.p0s + 3 * s + 1),
+                         rz = pz - __ldg(P.p0s + 3 * s + 2);
+            const double inv = rsqrt(rx * rx + ry * ry + rz * rz);
+            const double inv3 = inv * inv * inv;
+            tx += (ky * rz - kz * ry) * inv3;
+            ty += (kz * rx - kx * rz) * inv3;
+            tz += (kx * ry - ky * rx) * inv3;
+        }
+        bx += tx;
+        by += ty;
+        bz += tz;
+    }
+    double *red = sm.red + (warp * 32 + lane) * 3;
+    red[0] = bx;
+    red[1] = by;
+    red[2] = bz;
+    __syncthreads();
+    if (warp == 0) {
+        double sx = 0.0, sy = 0.0, sz = 0.0;
+        for (int w = 0; w < kTrackWarps; ++w) {
+            const double *r = sm.red + (w * 32 + lane) * 3;
+            sx += r[0];
+            sy += r[1];
+            sz += r[2];
+        }
+        double *out = P.partial + (u * 32 + lane) * 3;
+        out[0] = sx;
+        out[1] = sy;
+        out[2] = sz;
+    }
+    __syncthreads();
+}
+
+// Phase A, FP32c: the chunk's tiles stream through the shared-memory ring (TMA).
+// `kt` counts the tiles this CTA has consumed so far (ring slot and phase parity).
+// Returns false if a TMA wait gave up (CCT_ERR_TIMEOUT recorded).
+template <int PPT>
+static __device__ bool unit_field_f32c(const TrackParams &P, int64_t u, TrackSmem &sm, uint32_t &kt) {
+    const UnitRef U = locate_unit(P, u);
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int G = P.G;
+    const int NB = G / (32 * PPT);                 // particle sub-blocks
+    const int S = kTrackWarps / NB;                // slices of each tile
+    const int sb = warp % NB, sl = warp / NB;
+    const int g0 = sl * (kTile / 4 / S), g1 = g0 + kTile / 4 / S;
+
+    float ph[PPT][3], pl[PPT][3];
+#pragma unroll
+    for (int i = 0; i < PPT; ++i) {
+        int64_t j = U.b * G + sb * 32 * PPT + i * 32 + lane;
+        if (j >= P.n_p) j = P.n_p - 1;
+        const double *Ys = P.state + ((int64_t)U.d * P.n_p + j) * kStateD + ST_YS;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) split_df(Ys[c], ph[i][c], pl[i][c]);
+    }
+    F32cAcc<PPT> acc;
+    acc.zero();
+
+    const unsigned char *tiles = P.tiles + (P.tile_off[U.d] + U.t_beg) * (int64_t)kTileBytes;
+    const int64_t nt = U.t_end - U.t_beg;
+    if (tid == 0) {
+        for (int64_t t = 0; t < kRing && t < nt; ++t) {
+            const int s = (int)((kt + t) % kRing);
+            cctdev::fence_proxy_async();
+            cctdev::mbar_arrive_expect_tx(&sm.full[s], kTileBytes);
+            cctdev::bulk_g2s(sm.ring[s], tiles + t * (int64_t)kTileBytes, kTileBytes, &sm.full[s]);
+        }
+    }
+    bool ok_all = true;
+    for (int64_t t = 0; t < nt; ++t) {
+        const uint32_t k = kt + (uint32_t)t;
+        const int s = (int)(k % kRing);
+        const bool ok = cctdev::mbar_wait_bounded(&sm.full[s], (k / kRing) & 1u, kTmaPolls);
+        if (__syncthreads_or(!ok)) {   // also: all threads are done with tile t-1
+            ok_all = false;
+            break;
+        }
+        if (tid == 0 && t >= 1 && t - 1 + kRing < nt) {
+            const int sp = (int)((k - 1) % kRing);
+            cctdev::fence_proxy_async();
+            cctdev::mbar_arrive_expect_tx(&sm.full[sp], kTileBytes);
+            cctdev::bulk_g2s(sm.ring[sp], tiles + (t - 1 + kRing) * (int64_t)kTileBytes, kTileBytes, &sm.full[sp]);
+        }
+        tile_f32c<PPT>(sm.ring[s], ph, pl, acc, g0, g1);
+    }
+    if (!ok_all) {
+        if (tid == 0) {
+            set_timeout(P);
+            for (int s = 0; s < kRing; ++s) (void)cctdev::mbar_wait_bounded(&sm.full[s], 0, 1024);
+        }
+        __syncthreads();
+        return false;
+    }
+    kt += (uint32_t)nt;
+
+    // reduce the S slices of every particle in fixed order
+#pragma unroll
+    for (int i = 0; i < PPT; ++i) {
+        double *r = sm.red + ((size_t)sl * G + sb * 32 * PPT + i * 32 + lane) * 3;
+        r[0] = acc.total(i, 0);
+        r[1] = acc.total(i, 1);
+        r[2] = acc.total(i, 2);
+    }
+    __syncthreads();
+    for (int slot = tid; slot < G; slot += kTrackBlock) {
+        double sx = 0.0, sy = 0.0, sz = 0.0;
+        for (int q = 0; q < S; ++q) {
+            const double *r = sm.red + ((size_t)q * G + slot) * 3;
+            sx += r[0];
+            sy += r[1];
+            sz += r[2];
+        }
+        double *out = P.partial + (u * G + slot) * 3;
+        out[0] = sx;
+        out[1] = sy;
+        out[2] = sz;
+    }
+    __syncthreads();
+    return true;
+}
+
+// Phase C for one particle at RK4 stage `stage` (0..3) of step `step`.
+static __device__ void particle_update(const TrackParams &P, int64_t pi, int step, int stage) {
+    double *S = P.state + pi * kStateD;
+    if ((double)step >= S[ST_NSTEPS]) return;
+    const int d = (int)(pi / P.n_p);
+    const int64_t j = pi % P.n_p;
+    const int64_t b = j / P.G, slot = j % P.G;
+    const int64_t cd = P.chunks[d];
+    const int64_t u0 = P.unit_off[d] + b * cd;
+    double B[3] = {0.0, 0.0, 0.0};
+    for (int64_t c = 0; c < cd; ++c) {
+        const double *p = P.partial + ((u0 + c) * P.G + slot) * 3;
+        B[0] += p[0];
+        B[1] += p[1];
+        B[2] += p[2];
+    }
+    const double *Ys = S + ST_YS;
+    for (int64_t q = P.qs_off[d]; q < P.qs_off[d + 1]; ++q)
+        qs_field_add(P.qs + kQsRecord * q, Ys[0], Ys[1], Ys[2], B[0], B[1], B[2]);
+    if (P.record) {
+        double *rec = P.record + (((int64_t)(step - P.step_begin) * 4 + stage) * ((int64_t)P.n_designs * P.n_p) + pi) * kRec;
+        for (int c = 0; c < 6; ++c) rec[c] = Ys[c];
+        rec[6] = B[0];
+        rec[7] = B[1];
+        rec[8] = B[2];
+    }
+
+    // k = [v_s, kq * (v_s x B)]
+    double k[6];
+    k[0] = Ys[3];
+    k[1] = Ys[4];
+    k[2] = Ys[5];
+    double ax, ay, az;
+    cross_rn(Ys[3], Ys[4], Ys[5], B[0], B[1], B[2], ax, ay, az);
+    const double kq = S[ST_KQ];
+    k[3] = __dmul_rn(ax, kq);
+    k[4] = __dmul_rn(ay, kq);
+    k[5] = __dmul_rn(az, kq);
+
+    const double dt = S[ST_DT];
+    double *Y0 = S + ST_Y0, *Yn = S + ST_YS, *ks = S + ST_KSUM;
+    if (stage == 0) {
+        const double h = dt / 2;
+        for (int c = 0; c < 6; ++c) {
+            ks[c] = k[c];
+            Yn[c] = __dadd_rn(Y0[c], __dmul_rn(h, k[c]));
+        }
+    } else if (stage == 1 || stage == 2) {
+        const double h = stage == 1 ? dt / 2 : dt;
+        for (int c = 0; c < 6; ++c) {
+            ks[c] = __dadd_rn(ks[c], __dmul_rn(2.0, k[c]));
+            Yn[c] = __dadd_rn(Y0[c], __dmul_rn(h, k[c]));
+        }
+    } else {
+        const double h = dt / 6;
+        bool finite = true;
+        for (int c = 0; c < 6; ++c) {
+            ks[c] = __dadd_rn(ks[c], k[c]);
+            Y0[c] = __dadd_rn(Y0[c], __dmul_rn(h, ks[c]));
+            Yn[c] = Y0[c];
+            finite = finite && isfinite(Y0[c]);
+        }
+        if (!finite) atomicExch(P.ctrl + CW_NONFINITE, 1u);
+    }
+}
+
+// ---------------------------------------------------------------- host helpers (track.cu)
+extern int g_test_phantom_blocks;
+extern long long g_wait_ms;
+int group_size(int precision, int64_t n_p);
+int track_grid(int *grid_out);
+int64_t plan_units(const int64_t *hoff, int n_designs, int64_t n_p, int G, int grid, int64_t *unit_off,
+                   int64_t *chunks, int64_t *chunk_tiles);
+cudaError_t launch_track_kernel(TrackParams &P, int grid, cudaStream_t st);
+
+}  // namespace cctgpu

@@ -121,6 +121,32 @@ int cct_track(const double *d_kls, const double *d_p0s, const int64_t *d_seg_off
               double distance, double footstep, int32_t precision,
               void *d_scratch, int64_t scratch_bytes, void *stream);
 
+/* ---------------------------------------------------------------------------
+ * Adjoint (gradients): no counterpart in the reference, which has no
+ * derivatives; it differentiates cct_track's FP64 forward (the reference's RK4
+ * with the midpoint Biot-Savart field, particles.py:515-596, cct.py:249-285).
+ * Objective per design d over its particles' final positions p_i, with the
+ * exit frame d_exit_frame[9*d..] = (o, XI, YI) of the ideal particle:
+ *   J_d = mean_i (x_i^2 + y_i^2),  x_i = XI.(p_i - o),  y_i = YI.(p_i - o)
+ * (RMS spot size squared plus centroid squared, both planes).  Writes J_d to
+ * d_J[d] and dJ_d/d(kl_i) (3), dJ_d/d(p0_i) (3) of every segment i of design d
+ * to d_seg_grad[6*i..] (the caller maps them to design parameters through the
+ * segment-generation Jacobian).  Discrete adjoint of the exact RK4 map, with
+ * the state checkpointed every `checkpoint_steps` steps and each segment of
+ * steps recomputed once.  Particles are tracked as by cct_track (precision 0)
+ * and their final records written to d_particles.  Scratch: at least
+ * cct_adjoint_scratch_bytes(n_designs, n_particles, steps, checkpoint_steps)
+ * bytes, `steps` an upper bound of any particle's step count.  Synchronous. */
+int64_t cct_adjoint_scratch_bytes(int32_t n_designs, int64_t n_particles,
+                                  int32_t max_steps, int32_t checkpoint_steps);
+int cct_track_adjoint(const double *d_kls, const double *d_p0s,
+                      const int64_t *d_seg_off, const double *d_qs,
+                      const int64_t *d_qs_off, int32_t n_designs,
+                      double *d_particles, int64_t n_particles, double distance,
+                      double footstep, const double *d_exit_frame, double *d_J,
+                      double *d_seg_grad, int32_t checkpoint_steps,
+                      void *d_scratch, int64_t scratch_bytes, void *stream);
+
 /* cct_track without any device allocation, for callers that may not allocate
  * device memory once running (memory reserved up front by a host application;
  * a C caller that owns only the buffers it passes).  No counterpart in the

@@ -1,0 +1,141 @@
+"""Adjoint gradients (cct_track_adjoint + the complex-step segment Jacobian) against
+central finite differences, h = 1e-4 relative: of the GPU FP64 forward, of the CPU
+oracle (reduced magnet), and of the 13-parameter gantry design."""
+import math
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+from cctpy_gb300 import CCT, engine, workloads as W
+from cctpy_gb300.adjoint import (BeamObjective, GantryDesign, design_gradients, exit_frame, layer_gradient,
+                                 objective_host, segment_gradient)
+from oracle import cct_oracle as O
+
+H_REL = 1e-4
+GRAD_RTOL = 1e-5
+
+
+def clone(c: CCT, tilts=None, current=None, big_r=None, dpw=None, winding=None) -> CCT:
+    return CCT(c.local_coordinate_system, c.big_r if big_r is None else big_r, c.small_r, c.bending_angle,
+               c.tilt_angles if tilts is None else tilts, c.winding_number if winding is None else winding,
+               c.current if current is None else current, c.starting_point_in_ksi_phi_coordinate,
+               c.end_point_in_ksi_phi_coordinate, c.disperse_number_per_winding if dpw is None else dpw)
+
+
+def params_of(c: CCT):
+    return list(c.tilt_angles) + [c.current, c.big_r]
+
+
+def with_params(c: CCT, v):
+    return clone(c, tilts=list(v[:-2]), current=v[-2], big_r=v[-1])
+
+
+def flat(lg):
+    return np.array(list(lg["tilt"]) + [lg["current"], lg["big_r"]])
+
+
+def check_close(g_adj, g_fd):
+    scale = np.abs(g_fd).max()
+    err = np.abs(g_adj - g_fd)
+    assert np.all(err <= GRAD_RTOL * np.abs(g_fd) + 1e-7 * scale), (g_adj, g_fd, err / np.maximum(np.abs(g_fd), 1e-300))
+
+
+def test_adjoint_matches_gpu_central_differences():
+    traj, base = W.build_single_dipole()
+    c0 = W.SINGLE_DIPOLE
+    ps = W.single_dipole_particles(16, seed=4)
+    L, step = 0.1, 0.002
+    frame = exit_frame(traj, c0["drift"] + L, c0["kinetic_MeV"])
+    J, seg, final = segment_gradient(engine.design_of(base), ps, L, step, frame[None, :], checkpoint=16)
+    J_fwd = objective_host(engine.track(engine.design_of(base), ps, L, step, "f64")[0], frame)
+    assert abs(J[0] - J_fwd) <= 1e-12 * J_fwd
+    g_adj = flat(layer_gradient(base, seg))
+    v0 = params_of(base)
+    g_fd = np.zeros(len(v0))
+    for k in range(len(v0)):
+        h = H_REL * abs(v0[k])
+        Jk = []
+        for sgn in (1, -1):
+            v = list(v0)
+            v[k] += sgn * h
+            m = with_params(base, v)
+            Jk.append(objective_host(engine.track(engine.design_of(m), ps, L, step, "f64")[0], frame))
+        g_fd[k] = (Jk[0] - Jk[1]) / (2 * h)
+    check_close(g_adj, g_fd)
+
+
+def test_adjoint_matches_oracle_central_differences():
+    traj, base = W.build_single_dipole()
+    small = clone(base, winding=8, dpw=36)        # 288 segments: the oracle finishes in seconds
+    c0 = W.SINGLE_DIPOLE
+    ps = W.single_dipole_particles(4, seed=6)
+    L, step = 0.02, 0.002
+    frame = exit_frame(traj, c0["drift"] + L, c0["kinetic_MeV"])
+    _, seg, _ = segment_gradient(engine.design_of(small), ps, L, step, frame[None, :], checkpoint=4)
+    g_adj = flat(layer_gradient(small, seg))
+
+    def oracle_J(m: CCT) -> float:
+        lcs = m.local_coordinate_system
+        fr = O.Frame.from_axes(*[tuple(r) for r in lcs.axes()])
+        rec = O.cct_record(fr, m.big_r, m.small_r, m.bending_angle, m.tilt_angles, m.winding_number, m.current,
+                           (m.starting_point_in_ksi_phi_coordinate.x, m.starting_point_in_ksi_phi_coordinate.y),
+                           (m.end_point_in_ksi_phi_coordinate.x, m.end_point_in_ksi_phi_coordinate.y),
+                           m.disperse_number_per_winding)
+        mo = O.CCTOracle(rec)
+        return objective_host(np.array([O.rk4_track(p, mo.field_at, L, step) for p in ps]), frame)
+
+    v0 = params_of(small)
+    g_fd = np.zeros(len(v0))
+    for k in range(len(v0)):
+        h = H_REL * abs(v0[k])
+        vp, vm = list(v0), list(v0)
+        vp[k] += h
+        vm[k] -= h
+        g_fd[k] = (oracle_J(with_params(small, vp)) - oracle_J(with_params(small, vm))) / (2 * h)
+    check_close(g_adj, g_fd)
+
+
+def test_gantry_design_gradient_matches_central_differences():
+    kw = W.design_population(1, seed=3)[0]
+    theta = np.array(kw["dicct345_tilt_angles"] + kw["agcct345_tilt_angles"]
+                     + [kw["dicct345_current"], kw["dicct345_current"], kw["agcct345_current"],
+                        kw["agcct345_current"], 0.95])
+    dpw = 60
+    base = GantryDesign(theta, part_per_winding=dpw)
+    ps = W.beam_particles(base.beamline, 8, seed=7, kinetic_MeV=215.0)
+    L, step = 0.3, 0.01
+    J, g = design_gradients([base], ps, L, step, 215.0, checkpoint=8)
+    frame = exit_frame(base.beamline.trajectory, L, 215.0)
+    for k in (1, 6, 9, 10, 12):     # a dipole tilt, an AG tilt, two currents, the winding radius
+        h = H_REL * abs(theta[k])
+        Jk = []
+        for sgn in (1, -1):
+            t = theta.copy()
+            t[k] += sgn * h
+            d = GantryDesign(t, part_per_winding=dpw)
+            Jk.append(objective_host(engine.track(engine.design_of(d.beamline), ps, L, step, "f64")[0], frame))
+        fd = (Jk[0] - Jk[1]) / (2 * h)
+        assert abs(g[0, k] - fd) <= GRAD_RTOL * abs(fd) + 1e-7 * np.abs(g[0]).max(), (k, g[0, k], fd)
+
+
+def test_autograd_function_and_batched_designs():
+    designs = W.design_population(2, seed=3)
+    theta = torch.tensor([kw["dicct345_tilt_angles"] + kw["agcct345_tilt_angles"]
+                          + [kw["dicct345_current"], kw["dicct345_current"], kw["agcct345_current"],
+                             kw["agcct345_current"], 0.95] for kw in designs], dtype=torch.float64,
+                         requires_grad=True)
+    bl0 = GantryDesign(theta[0].detach().numpy(), part_per_winding=60).beamline
+    ps = W.beam_particles(bl0, 4, seed=8, kinetic_MeV=215.0)
+    J = BeamObjective.apply(theta, ps, 0.1, 0.01, 215.0, 60)
+    J.sum().backward()
+    J2, g2 = design_gradients([GantryDesign(t, part_per_winding=60) for t in theta.detach().numpy()], ps, 0.1,
+                              0.01, 215.0)
+    np.testing.assert_allclose(J.detach().numpy(), J2, rtol=1e-14)
+    np.testing.assert_allclose(theta.grad.numpy(), g2, rtol=1e-12)
+    # each design's gradient equals the one of a single-design run
+    _, g0 = design_gradients([GantryDesign(theta[0].detach().numpy(), part_per_winding=60)], ps, 0.1, 0.01, 215.0)
+    np.testing.assert_allclose(g2[0], g0[0], rtol=1e-12, atol=0)
