@@ -189,6 +189,40 @@ def measure_tracking(args, dev, rank):
                         "one launch",
             "f32c": {"steps": s32 // 2, "seconds": tp, "particle_steps_per_s": rp,
                      "gpairs_per_s": 512 * (s32 // 2) * 4 * dsp.n_segments / tp / 1e9}}
+    if not args.no_adjoint:
+        out["design_gradients"] = measure_design_grads(args, rank)
+    return out
+
+
+def measure_design_grads(args, rank):
+    """design-grads/s: 13-parameter gradients of J = <x^2> + <y^2> at the exit for 16 gantry
+    designs x 1024 protons in one adjoint run (FP32c forward + FP32c adjoint sweeps, and the
+    FP64 adjoint on fewer steps), on a slice of args.adjoint_steps 1 mm RK4 steps."""
+    import torch
+    from cctpy_gb300 import workloads as W
+    from cctpy_gb300.adjoint import GantryDesign, design_gradients
+
+    kws = W.design_population(16, seed=3)
+    thetas = [np.array(kw["dicct345_tilt_angles"] + kw["agcct345_tilt_angles"]
+                       + [kw["dicct345_current"], kw["dicct345_current"], kw["agcct345_current"],
+                          kw["agcct345_current"], 0.95]) for kw in kws]
+    designs = [GantryDesign(t, part_per_winding=360) for t in thetas]
+    ps = W.beam_particles(designs[0].beamline, 1024, seed=4 + rank, kinetic_MeV=215.0)
+    n_seg = sum(sum(m.total_disperse_number for m in d.beamline.magnets if hasattr(m, "winding_number"))
+                for d in designs)
+    out = {"workload": f"16 second-section designs ({n_seg} segments total), 1024 protons each, 13 parameters "
+                       "(8 tilts, 4 layer currents, winding radius), J = <x^2>+<y^2> at the exit; "
+                       "adjoint with checkpoints every 16 steps"}
+    for prec, steps in (("f32c", args.adjoint_steps), ("f64", max(1, args.adjoint_steps // 16))):
+        design_gradients(designs, ps, 0.002, 0.001, 215.0, checkpoint=16, precision=prec)   # warm-up
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        J, g = design_gradients(designs, ps, steps * 0.001, 0.001, 215.0, checkpoint=16, precision=prec)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        out[prec] = {"steps": steps, "seconds": dt, "design_grads_per_s": len(designs) / dt,
+                     "design_grad_steps_per_s": len(designs) * steps / dt,
+                     "gradient_norm_design0": float(np.linalg.norm(g[0]))}
     return out
 
 
@@ -375,6 +409,8 @@ def main():
     ap.add_argument("--no-tracking", action="store_true")
     ap.add_argument("--no-population", action="store_true")
     ap.add_argument("--track-steps", type=int, default=20, help="timed FP32c RK4 steps of the tracking slice")
+    ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--adjoint-steps", type=int, default=32, help="RK4 steps of the design-gradient slice")
     ap.add_argument("--traffic", type=float, default=None,
                     help="DRAM bytes per launch of the timed kernel from an ncu capture")
     args = ap.parse_args()

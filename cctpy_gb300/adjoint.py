@@ -52,8 +52,9 @@ def objective_host(final: np.ndarray, frame: np.ndarray) -> float:
 
 
 def segment_gradient(ds: engine.DesignSet, particles, distance: float, footstep: float, frames: np.ndarray,
-                     checkpoint: int = 64):
-    """(J (D,), dJ/d(kl, p0) (N_seg, 6), final records (D, n, 10)) for the designs of `ds`."""
+                     checkpoint: int = 64, precision: str = "f64"):
+    """(J (D,), dJ/d(kl, p0) (N_seg, 6), final records (D, n, 10)) for the designs of `ds`;
+    precision "f64" or "f32c" (forward and adjoint sweeps)."""
     lib = _lib.load()
     dev = ds.kls.device
     p = torch.as_tensor(np.asarray(particles, dtype=np.float64), device=dev)
@@ -70,10 +71,14 @@ def segment_gradient(ds: engine.DesignSet, particles, distance: float, footstep:
     grad = torch.empty((max(ds.n_segments, 1), 6), dtype=torch.float64, device=dev)
     nbytes = lib.cct_adjoint_scratch_bytes(ds.n_designs, n_p, max_steps, checkpoint)
     _lib.check(0 if nbytes >= 0 else _lib.CCT_ERR_ARG, "cct_adjoint_scratch_bytes")
+    prec = {"f64": 0, "f32c": 1}.get(precision)
+    if prec is None:
+        raise ValueError(f"precision must be 'f64' or 'f32c', not {precision!r}")
+    packed = ds.packed().data_ptr() if prec == 1 else 0
     sc = engine.scratch(nbytes, dev)
-    rc = lib.cct_track_adjoint(engine._ptr(ds.kls), engine._ptr(ds.p0s), engine._ptr(ds.seg_off),
+    rc = lib.cct_track_adjoint(engine._ptr(ds.kls), engine._ptr(ds.p0s), engine._ptr(ds.seg_off), packed,
                                engine._ptr(ds.qs), engine._ptr(ds.qs_off), ds.n_designs, p.data_ptr(), n_p,
-                               float(distance), float(footstep), fr.data_ptr(), J.data_ptr(), grad.data_ptr(),
+                               float(distance), float(footstep), prec, fr.data_ptr(), J.data_ptr(), grad.data_ptr(),
                                int(checkpoint), sc.data_ptr(), int(nbytes), engine._stream())
     _lib.check(rc, "cct_track_adjoint")
     return J.cpu().numpy(), grad[:ds.n_segments].cpu().numpy(), p.cpu().numpy()
@@ -190,13 +195,14 @@ class GantryDesign:
 
 
 def design_gradients(designs: Sequence[GantryDesign], particles: np.ndarray, distance: float, footstep: float,
-                     kinetic_MeV: float, checkpoint: int = 64) -> Tuple[np.ndarray, np.ndarray]:
+                     kinetic_MeV: float, checkpoint: int = 64, precision: str = "f64") -> Tuple[np.ndarray, np.ndarray]:
     """J (D,) and dJ/dtheta (D, 13) of every design, all tracked in one adjoint run.  The
     designs share the design orbit: particles start at s = 0 and the objective is read in
     the ideal particle's frame at s = distance."""
     ds = engine.design_set_of([d.beamline for d in designs])
     frame = exit_frame(designs[0].beamline.trajectory, distance, kinetic_MeV)
-    J, seg, _ = segment_gradient(ds, particles, distance, footstep, np.tile(frame, (len(designs), 1)), checkpoint)
+    J, seg, _ = segment_gradient(ds, particles, distance, footstep, np.tile(frame, (len(designs), 1)), checkpoint,
+                                 precision)
     grads = np.zeros((len(designs), 13))
     for d, des in enumerate(designs):
         a, b = int(ds.h_seg_off[d]), int(ds.h_seg_off[d + 1])

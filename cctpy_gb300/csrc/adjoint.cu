@@ -24,7 +24,8 @@
 // (adjoint_kernel: phase A' sums (dB/dp)^T a over segment chunks per particle block, as the
 // forward's phase A sums B; phase C' advances the lambdas), and accumulate the segment
 // gradient from the recorded (p, a) pairs (seg_adjoint_kernel, one thread per segment).
-// The adjoint sweeps run in FP64.
+// The sweeps run in the forward's precision: FP64, or FP32c (packed FP32 pair terms on the
+// tile-local frames, Kahan-compensated, as the forward field sums).
 #include <algorithm>
 #include <vector>
 
@@ -234,11 +235,22 @@ __global__ void __launch_bounds__(kTrackBlock) adjoint_kernel(AdjParams A) {
     const int64_t n_units = P.unit_off[P.n_designs];
     const int64_t first = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (A.step_end <= A.step_begin) return;
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < kRing; ++s) cctdev::mbar_init(&sm.full[s], 1);
+        cctdev::mbar_fence_init();
+    }
     for (int64_t pi = first; pi < total; pi += tstride) begin_step(A, pi, A.step_end - 1);
     if (!grid_barrier(P, sm)) return;
+    uint32_t kt = 0;   // tiles consumed through the TMA ring by this CTA (FP32c)
     for (int step = A.step_end - 1; step >= A.step_begin; --step) {
         for (int stage = 3; stage >= 0; --stage) {
-            for (int64_t u = blockIdx.x; u < n_units; u += gridDim.x) unit_grad_f64(A, u, step, stage, sm);
+            const PointSrc src{rec_at(P, step, stage, 0), kRec, A.adj + AD_A, kAdjD};
+            bool ok = true;
+            for (int64_t u = blockIdx.x; u < n_units && ok; u += gridDim.x) {
+                if (P.precision == 0) unit_grad_f64(A, u, step, stage, sm);
+                else if (P.ppt == 2) ok = unit_sum_f32c<2, true>(P, src, u, sm, kt);
+                else ok = unit_sum_f32c<1, true>(P, src, u, sm, kt);
+            }
             if (!grid_barrier(P, sm)) return;
             for (int64_t pi = first; pi < total; pi += tstride) {
                 end_stage(A, pi, step, stage);
@@ -319,6 +331,124 @@ __global__ void __launch_bounds__(kSegBlock) seg_adjoint_kernel(TrackParams P, i
     }
 }
 
+// FP32c segment gradient: one warp per packed tile, four segments per lane (two packed
+// pairs); the design's recorded (p, a) pairs are staged in shared memory in the tile's local
+// double-float frame, 128 at a time; per-chunk FP32 sums are Kahan-compensated per segment.
+constexpr int kSegPts = 128;
+
+__global__ void __launch_bounds__(32) seg_adjoint_f32c_kernel(TrackParams P, int n_steps, double *grad) {
+    __shared__ __align__(16) f2 pts[kSegPts][9];   // (q,q) x3, (a,a) x3, (-a,-a) x3
+    const int64_t t = blockIdx.x;
+    int lo = 0, hi = P.n_designs - 1;               // design of tile t: last d with tile_off[d] <= t
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) / 2;
+        if (P.tile_off[mid] <= t) lo = mid; else hi = mid - 1;
+    }
+    const int d = lo;
+    const unsigned char *tile = P.tiles + t * (int64_t)kTileBytes;
+    const TileHeader *h = reinterpret_cast<const TileHeader *>(tile);
+    const ulonglong2 *v = reinterpret_cast<const ulonglong2 *>(tile + kTileHeaderBytes);
+    constexpr int Q = kTile / 4;
+    const int lane = threadIdx.x;
+    const int cnt = h->count;
+    const int64_t s0 = P.seg_off[d] + (t - P.tile_off[d]) * kTile;
+    ulonglong2 K[9];
+#pragma unroll
+    for (int c = 0; c < 9; ++c) K[c] = v[c * Q + lane];
+    float S[4][6], C[4][6];
+#pragma unroll
+    for (int m = 0; m < 4; ++m)
+#pragma unroll
+        for (int c = 0; c < 6; ++c) S[m][c] = C[m][c] = 0.0f;
+    const f2 m3 = f2_pack(-3.0f, -3.0f);
+    const int64_t total = (int64_t)P.n_designs * P.n_p;
+    const int64_t n_pts = (int64_t)n_steps * 4 * P.n_p;
+    for (int64_t base = 0; base < n_pts; base += kSegPts) {
+        __syncthreads();
+        for (int k = lane; k < kSegPts; k += 32) {
+            const int64_t e = base + k;
+            float q[3] = {0.f, 0.f, 0.f}, a[3] = {0.f, 0.f, 0.f};
+            if (e < n_pts) {
+                const double *r = P.record + ((e / P.n_p) * total + (int64_t)d * P.n_p + e % P.n_p) * kRec;
+                for (int c = 0; c < 3; ++c) {
+                    float ph, pl;
+                    split_df(r[c], ph, pl);
+                    q[c] = __fadd_rn(__fsub_rn(ph, h->o_hi[c]), __fsub_rn(pl, h->o_lo[c]));
+                    a[c] = (float)r[9 + c];
+                }
+            }
+            for (int c = 0; c < 3; ++c) {
+                pts[k][c] = f2_pack(q[c], q[c]);
+                pts[k][3 + c] = f2_pack(a[c], a[c]);
+                pts[k][6 + c] = f2_pack(-a[c], -a[c]);
+            }
+        }
+        __syncthreads();
+        f2 KL[2][3], PZ[2][3];
+#pragma unroll
+        for (int m = 0; m < 2; ++m)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) KL[m][c] = PZ[m][c] = 0ull;
+        const int np = (int)min((int64_t)kSegPts, n_pts - base);
+#pragma unroll 1
+        for (int i = 0; i < np; ++i) {
+            const f2 Ax = pts[i][3], Ay = pts[i][4], Az = pts[i][5];
+            if ((Ax | Ay | Az) == 0ull) continue;              // inactive stage: uniform over the warp
+            const f2 Qx = pts[i][0], Qy = pts[i][1], Qz = pts[i][2];
+            const f2 NAx = pts[i][6], NAy = pts[i][7], NAz = pts[i][8];
+#pragma unroll
+            for (int m = 0; m < 2; ++m) {
+                const f2 kx = m ? K[0].y : K[0].x, ky = m ? K[1].y : K[1].x, kz = m ? K[2].y : K[2].x;
+                const f2 nx = m ? K[3].y : K[3].x, ny = m ? K[4].y : K[4].x, nz = m ? K[5].y : K[5].x;
+                const f2 px = m ? K[6].y : K[6].x, py = m ? K[7].y : K[7].x, pz = m ? K[8].y : K[8].x;
+                const f2 rx = f2_sub(Qx, px), ry = f2_sub(Qy, py), rz = f2_sub(Qz, pz);
+                const f2 r2 = f2_fma(rx, rx, f2_fma(ry, ry, f2_mul(rz, rz)));
+                float l0, l1;
+                f2_unpack(r2, l0, l1);
+                const f2 inv = f2_pack(rsqrt_mufu(l0), rsqrt_mufu(l1));
+                const f2 inv2 = f2_mul(inv, inv);
+                const f2 inv3 = f2_mul(inv2, inv);
+                const f2 m3inv5 = f2_mul(f2_mul(inv3, inv2), m3);
+                // r x a
+                const f2 rax = f2_fma(ry, Az, f2_mul(rz, NAy));
+                const f2 ray = f2_fma(rz, Ax, f2_mul(rx, NAz));
+                const f2 raz = f2_fma(rx, Ay, f2_mul(ry, NAx));
+                KL[m][0] = f2_fma(rax, inv3, KL[m][0]);
+                KL[m][1] = f2_fma(ray, inv3, KL[m][1]);
+                KL[m][2] = f2_fma(raz, inv3, KL[m][2]);
+                // c = a x kl; grad_p (a . B_i) = c inv3 - 3 (c.r) inv5 r
+                const f2 cx = f2_fma(Ay, kz, f2_mul(Az, ny));
+                const f2 cy = f2_fma(Az, kx, f2_mul(Ax, nz));
+                const f2 cz = f2_fma(Ax, ky, f2_mul(Ay, nx));
+                const f2 nq = f2_mul(f2_fma(cx, rx, f2_fma(cy, ry, f2_mul(cz, rz))), m3inv5);
+                PZ[m][0] = f2_fma(nq, rx, f2_fma(cx, inv3, PZ[m][0]));
+                PZ[m][1] = f2_fma(nq, ry, f2_fma(cy, inv3, PZ[m][1]));
+                PZ[m][2] = f2_fma(nq, rz, f2_fma(cz, inv3, PZ[m][2]));
+            }
+        }
+#pragma unroll
+        for (int m = 0; m < 2; ++m)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                float e0, e1;
+                f2_unpack(KL[m][c], e0, e1);
+                kahan_add(S[2 * m][c], C[2 * m][c], e0);
+                kahan_add(S[2 * m + 1][c], C[2 * m + 1][c], e1);
+                f2_unpack(PZ[m][c], e0, e1);
+                kahan_add(S[2 * m][3 + c], C[2 * m][3 + c], e0);
+                kahan_add(S[2 * m + 1][3 + c], C[2 * m + 1][3 + c], e1);
+            }
+    }
+#pragma unroll
+    for (int m = 0; m < 4; ++m) {
+        const int j = 4 * lane + m;
+        if (j >= cnt) continue;
+        double *g = grad + 6 * (s0 + j);
+        for (int c = 0; c < 3; ++c) g[c] += (double)S[m][c] - (double)C[m][c];
+        for (int c = 0; c < 3; ++c) g[3 + c] -= (double)S[m][3 + c] - (double)C[m][3 + c];   // dJ/dp0 = -grad_p
+    }
+}
+
 // ---------------------------------------------------------------- host side
 struct AdjLayout {
     int64_t track_total, ckpt_off, record_off, adj_off, total;
@@ -353,20 +483,33 @@ static int64_t adjoint_scratch_bound(int n_designs, int64_t n_p, int max_steps, 
     return adj_layout(L, n_designs, n_p, n_ckpt, K).total;
 }
 
-static int launch_adjoint(const double *kls, const double *p0s, const int64_t *seg_off, const double *qs,
-                   const int64_t *qs_off, int n_designs, double *particles, int64_t n_p, double distance,
-                   double footstep, const double *exit_frame, double *J, double *seg_grad, int K, void *scratch,
-                   int64_t scratch_bytes, cudaStream_t st) {
+static int launch_adjoint(const double *kls, const double *p0s, const int64_t *seg_off, const void *packed,
+                          const double *qs, const int64_t *qs_off, int n_designs, double *particles, int64_t n_p,
+                          double distance, double footstep, int precision, const double *exit_frame, double *J,
+                          double *seg_grad, int K, void *scratch, int64_t scratch_bytes, cudaStream_t st) {
     std::vector<int64_t> hoff(n_designs + 1), tables(3 * n_designs + 1);
     CCT_TRY_CUDA(cudaMemcpyAsync(hoff.data(), seg_off, 8 * (n_designs + 1), cudaMemcpyDeviceToHost, st));
     CCT_TRY_CUDA(cudaStreamSynchronize(st));
     for (int d = 0; d < n_designs; ++d)
         if (hoff[d + 1] < hoff[d]) return set_error(CCT_ERR_ARG, "segment offsets decrease at design %d", d);
+    const unsigned char *tiles = nullptr;
+    const int64_t *tile_off = nullptr;
+    int64_t tiles_total = 0;
+    for (int d = 0; d < n_designs; ++d) tiles_total += (hoff[d + 1] - hoff[d] + kTile - 1) / kTile;
+    if (precision == 1) {
+        int64_t ph[3];
+        CCT_TRY_CUDA(cudaMemcpyAsync(ph, packed, sizeof ph, cudaMemcpyDeviceToHost, st));
+        CCT_TRY_CUDA(cudaStreamSynchronize(st));
+        if (ph[0] != kPackedMagic || ph[1] != n_designs || ph[2] != tiles_total)
+            return set_error(CCT_ERR_ARG, "packed segments do not match the %d designs' segment offsets", n_designs);
+        tile_off = reinterpret_cast<const int64_t *>(static_cast<const unsigned char *>(packed) + kPackedHeaderBytes);
+        tiles = static_cast<const unsigned char *>(packed) + kPackedHeaderBytes + packed_index_bytes(n_designs);
+    }
     int grid = 0, agrid = 0;
     int rc = track_grid(&grid);
     if (rc == CCT_OK) rc = adjoint_grid(&agrid);
     if (rc != CCT_OK) return rc;
-    const int G = group_size(0, n_p);
+    const int G = group_size(precision, n_p);
     int64_t *unit_off = tables.data(), *chunks = unit_off + n_designs + 1, *chunk_tiles = chunks + n_designs;
     const int64_t n_units = plan_units(hoff.data(), n_designs, n_p, G, grid, unit_off, chunks, chunk_tiles);
     const TrackScratchLayout L = track_scratch_layout(n_designs, n_p, n_units, G);
@@ -379,13 +522,13 @@ static int launch_adjoint(const double *kls, const double *p0s, const int64_t *s
     P.kls = kls;
     P.p0s = p0s;
     P.seg_off = seg_off;
-    P.tiles = nullptr;
-    P.tile_off = nullptr;
+    P.tiles = tiles;
+    P.tile_off = tile_off;
     P.qs = qs;
     P.qs_off = qs_off;
     P.n_designs = n_designs;
     P.G = G;
-    P.ppt = 1;
+    P.ppt = G >= 64 ? 2 : 1;
     P.n_p = n_p;
     P.particles = particles;
     P.distance = distance;
@@ -396,7 +539,7 @@ static int launch_adjoint(const double *kls, const double *p0s, const int64_t *s
     P.unit_off = reinterpret_cast<const int64_t *>(sc + 256);
     P.chunks = P.unit_off + n_designs + 1;
     P.chunk_tiles = P.chunks + n_designs;
-    P.precision = 0;
+    P.precision = precision;
     P.barrier_blocks = (unsigned)(grid + g_test_phantom_blocks);
     P.wait_ns = (unsigned long long)g_wait_ms * 1000000ull;
     P.record = nullptr;
@@ -464,7 +607,10 @@ static int launch_adjoint(const double *kls, const double *p0s, const int64_t *s
         void *args[] = {&A};
         CCT_TRY_CUDA(cudaLaunchCooperativeKernel((const void *)adjoint_kernel, dim3(agrid), dim3(kTrackBlock), args,
                                                  0, st));
-        if (max_seg > 0) {
+        if (precision == 1 && tiles_total > 0) {
+            seg_adjoint_f32c_kernel<<<(unsigned)tiles_total, 32, 0, st>>>(P, P.step_end - P.step_begin, seg_grad);
+            CCT_TRY_CUDA(cudaGetLastError());
+        } else if (precision == 0 && max_seg > 0) {
             const dim3 sg((unsigned)((max_seg + kSegBlock - 1) / kSegBlock), (unsigned)n_designs);
             seg_adjoint_kernel<<<sg, kSegBlock, 0, st>>>(P, P.step_end - P.step_begin, seg_grad);
             CCT_TRY_CUDA(cudaGetLastError());
@@ -493,19 +639,22 @@ extern "C" int64_t cct_adjoint_scratch_bytes(int32_t n_designs, int64_t n_partic
 }
 
 extern "C" int cct_track_adjoint(const double *d_kls, const double *d_p0s, const int64_t *d_seg_off,
-                                 const double *d_qs, const int64_t *d_qs_off, int32_t n_designs, double *d_particles,
-                                 int64_t n_particles, double distance, double footstep, const double *d_exit_frame,
-                                 double *d_J, double *d_seg_grad, int32_t checkpoint_steps, void *d_scratch,
-                                 int64_t scratch_bytes, void *stream) {
+                                 const void *d_packed, const double *d_qs, const int64_t *d_qs_off, int32_t n_designs,
+                                 double *d_particles, int64_t n_particles, double distance, double footstep,
+                                 int32_t precision, const double *d_exit_frame, double *d_J, double *d_seg_grad,
+                                 int32_t checkpoint_steps, void *d_scratch, int64_t scratch_bytes, void *stream) {
     using namespace cctgpu;
     clear_error();
     if (n_designs <= 0 || n_particles <= 0) return set_error(CCT_ERR_ARG, "need at least one design and particle");
     if (!(distance > 0.0) || !(footstep > 0.0))
         return set_error(CCT_ERR_ARG, "distance (%g) and footstep (%g) must be positive", distance, footstep);
+    if (precision != 0 && precision != 1) return set_error(CCT_ERR_ARG, "precision must be 0 or 1");
     if (!d_kls || !d_p0s || !d_seg_off || !d_qs_off || !d_particles || !d_exit_frame || !d_J || !d_seg_grad ||
         !d_scratch)
         return set_error(CCT_ERR_ARG, "null pointer");
-    return launch_adjoint(d_kls, d_p0s, d_seg_off, d_qs, d_qs_off, n_designs, d_particles, n_particles, distance,
-                          footstep, d_exit_frame, d_J, d_seg_grad, checkpoint_steps, d_scratch, scratch_bytes,
-                          static_cast<cudaStream_t>(stream));
+    if (precision == 1 && (!d_packed || reinterpret_cast<uintptr_t>(d_packed) % 256))
+        return set_error(CCT_ERR_ARG, "FP32c adjoint needs a 256-byte aligned packed buffer");
+    return launch_adjoint(d_kls, d_p0s, d_seg_off, d_packed, d_qs, d_qs_off, n_designs, d_particles, n_particles,
+                          distance, footstep, precision, d_exit_frame, d_J, d_seg_grad, checkpoint_steps, d_scratch,
+                          scratch_bytes, static_cast<cudaStream_t>(stream));
 }

@@ -144,3 +144,76 @@ __device__ __forceinline__ void split_df(double x, float &hi, float &lo) {
 }
 
 }  // namespace cctgpu
+
+namespace cctgpu {
+
+// Adjoint counterpart of tile_f32c: for PPT points with weights a (per point), accumulate
+// grad_p (a . B_i) = c |r|^-3 - 3 (c.r) r |r|^-5, c = a x kl_i, over segments [4*g0, 4*g1)
+// of one tile, with the same compensation (FP32 sub-blocks of <= 64 segments, Kahan (S, C)).
+template <int PPT>
+__device__ __forceinline__ void tile_grad_f32c(const unsigned char *tile, const float (&ph)[PPT][3],
+                                               const float (&pl)[PPT][3], const float (&a)[PPT][3],
+                                               F32cAcc<PPT> &acc, int g0 = 0, int g1 = kTile / 4) {
+    const TileHeader *h = reinterpret_cast<const TileHeader *>(tile);
+    const ulonglong2 *v = reinterpret_cast<const ulonglong2 *>(tile + kTileHeaderBytes);
+    constexpr int Q = kTile / 4;
+    f2 q[PPT][3], A[PPT][3];
+#pragma unroll
+    for (int i = 0; i < PPT; ++i)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const float d = __fadd_rn(__fsub_rn(ph[i][c], h->o_hi[c]), __fsub_rn(pl[i][c], h->o_lo[c]));
+            q[i][c] = f2_pack(d, d);
+            A[i][c] = f2_pack(a[i][c], a[i][c]);
+        }
+    const f2 m3 = f2_pack(-3.0f, -3.0f);
+#pragma unroll 1
+    for (int sb = g0; sb < g1; sb += 16) {
+        const int se = min(sb + 16, g1);
+        f2 G[PPT][3];
+#pragma unroll
+        for (int i = 0; i < PPT; ++i) G[i][0] = G[i][1] = G[i][2] = 0ull;
+#pragma unroll 1
+        for (int j = sb; j < se; ++j) {
+            const ulonglong2 KX = v[0 * Q + j], KY = v[1 * Q + j], KZ = v[2 * Q + j];
+            const ulonglong2 NX = v[3 * Q + j], NY = v[4 * Q + j], NZ = v[5 * Q + j];
+            const ulonglong2 PX = v[6 * Q + j], PY = v[7 * Q + j], PZ = v[8 * Q + j];
+#pragma unroll
+            for (int hh = 0; hh < 2; ++hh) {
+                const f2 kx = hh ? KX.y : KX.x, ky = hh ? KY.y : KY.x, kz = hh ? KZ.y : KZ.x;
+                const f2 nx = hh ? NX.y : NX.x, ny = hh ? NY.y : NY.x, nz = hh ? NZ.y : NZ.x;
+                const f2 px = hh ? PX.y : PX.x, py = hh ? PY.y : PY.x, pz = hh ? PZ.y : PZ.x;
+#pragma unroll
+                for (int i = 0; i < PPT; ++i) {
+                    const f2 rx = f2_sub(q[i][0], px), ry = f2_sub(q[i][1], py), rz = f2_sub(q[i][2], pz);
+                    const f2 r2 = f2_fma(rx, rx, f2_fma(ry, ry, f2_mul(rz, rz)));
+                    float lo, hi;
+                    f2_unpack(r2, lo, hi);
+                    const f2 inv = f2_pack(rsqrt_mufu(lo), rsqrt_mufu(hi));
+                    const f2 inv2 = f2_mul(inv, inv);
+                    const f2 inv3 = f2_mul(inv2, inv);
+                    const f2 m3inv5 = f2_mul(f2_mul(inv3, inv2), m3);
+                    // c = a x kl = (ay kz - az ky, az kx - ax kz, ax ky - ay kx)
+                    const f2 cx = f2_fma(A[i][1], kz, f2_mul(A[i][2], ny));
+                    const f2 cy = f2_fma(A[i][2], kx, f2_mul(A[i][0], nz));
+                    const f2 cz = f2_fma(A[i][0], ky, f2_mul(A[i][1], nx));
+                    const f2 cr = f2_fma(cx, rx, f2_fma(cy, ry, f2_mul(cz, rz)));
+                    const f2 nq = f2_mul(cr, m3inv5);
+                    G[i][0] = f2_fma(nq, rx, f2_fma(cx, inv3, G[i][0]));
+                    G[i][1] = f2_fma(nq, ry, f2_fma(cy, inv3, G[i][1]));
+                    G[i][2] = f2_fma(nq, rz, f2_fma(cz, inv3, G[i][2]));
+                }
+            }
+        }
+#pragma unroll
+        for (int i = 0; i < PPT; ++i)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                float lo, hi;
+                f2_unpack(G[i][c], lo, hi);
+                kahan_add(acc.S[i][c], acc.C[i][c], __fadd_rn(lo, hi));
+            }
+    }
+}
+
+}  // namespace cctgpu

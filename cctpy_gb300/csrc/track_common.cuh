@@ -185,11 +185,26 @@ static __device__ void unit_field_f64(const TrackParams &P, int64_t u, TrackSmem
     __syncthreads();
 }
 
+// Where phase A reads its points: the position of particle pi is at pos + pi * pos_stride;
+// for the adjoint's gradient sums the per-point weight a is at w + pi * w_stride.
+struct PointSrc {
+    const double *pos;
+    int64_t pos_stride;
+    const double *w;
+    int64_t w_stride;
+};
+
+__device__ __forceinline__ PointSrc stage_points(const TrackParams &P) {
+    return PointSrc{P.state + ST_YS, kStateD, nullptr, 0};
+}
+
 // Phase A, FP32c: the chunk's tiles stream through the shared-memory ring (TMA).
-// `kt` counts the tiles this CTA has consumed so far (ring slot and phase parity).
-// Returns false if a TMA wait gave up (CCT_ERR_TIMEOUT recorded).
-template <int PPT>
-static __device__ bool unit_field_f32c(const TrackParams &P, int64_t u, TrackSmem &sm, uint32_t &kt) {
+// GRAD = false: field sums B at the points; GRAD = true: gradient sums grad_p (a . B) with
+// the per-point weights of `src`.  `kt` counts the tiles this CTA has consumed so far (ring
+// slot and phase parity).  Returns false if a TMA wait gave up (CCT_ERR_TIMEOUT recorded).
+template <int PPT, bool GRAD>
+static __device__ bool unit_sum_f32c(const TrackParams &P, const PointSrc &src, int64_t u, TrackSmem &sm,
+                                     uint32_t &kt) {
     const UnitRef U = locate_unit(P, u);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int G = P.G;
@@ -198,14 +213,19 @@ static __device__ bool unit_field_f32c(const TrackParams &P, int64_t u, TrackSme
     const int sb = warp % NB, sl = warp / NB;
     const int g0 = sl * (kTile / 4 / S), g1 = g0 + kTile / 4 / S;
 
-    float ph[PPT][3], pl[PPT][3];
+    float ph[PPT][3], pl[PPT][3], a[PPT][3];
 #pragma unroll
     for (int i = 0; i < PPT; ++i) {
         int64_t j = U.b * G + sb * 32 * PPT + i * 32 + lane;
         if (j >= P.n_p) j = P.n_p - 1;
-        const double *Ys = P.state + ((int64_t)U.d * P.n_p + j) * kStateD + ST_YS;
+        const int64_t pi = (int64_t)U.d * P.n_p + j;
+        const double *Ys = src.pos + pi * src.pos_stride;
 #pragma unroll
         for (int c = 0; c < 3; ++c) split_df(Ys[c], ph[i][c], pl[i][c]);
+        if (GRAD) {
+#pragma unroll
+            for (int c = 0; c < 3; ++c) a[i][c] = (float)src.w[pi * src.w_stride + c];
+        }
     }
     F32cAcc<PPT> acc;
     acc.zero();
@@ -235,7 +255,8 @@ static __device__ bool unit_field_f32c(const TrackParams &P, int64_t u, TrackSme
             cctdev::mbar_arrive_expect_tx(&sm.full[sp], kTileBytes);
             cctdev::bulk_g2s(sm.ring[sp], tiles + (t - 1 + kRing) * (int64_t)kTileBytes, kTileBytes, &sm.full[sp]);
         }
-        tile_f32c<PPT>(sm.ring[s], ph, pl, acc, g0, g1);
+        if (GRAD) tile_grad_f32c<PPT>(sm.ring[s], ph, pl, a, acc, g0, g1);
+        else tile_f32c<PPT>(sm.ring[s], ph, pl, acc, g0, g1);
     }
     if (!ok_all) {
         if (tid == 0) {
@@ -271,6 +292,11 @@ static __device__ bool unit_field_f32c(const TrackParams &P, int64_t u, TrackSme
     }
     __syncthreads();
     return true;
+}
+
+template <int PPT>
+static __device__ __forceinline__ bool unit_field_f32c(const TrackParams &P, int64_t u, TrackSmem &sm, uint32_t &kt) {
+    return unit_sum_f32c<PPT, false>(P, stage_points(P), u, sm, kt);
 }
 
 // Phase C for one particle at RK4 stage `stage` (0..3) of step `step`.

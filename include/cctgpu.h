@@ -133,17 +133,20 @@ int cct_track(const double *d_kls, const double *d_p0s, const int64_t *d_seg_off
  * to d_seg_grad[6*i..] (the caller maps them to design parameters through the
  * segment-generation Jacobian).  Discrete adjoint of the exact RK4 map, with
  * the state checkpointed every `checkpoint_steps` steps and each segment of
- * steps recomputed once.  Particles are tracked as by cct_track (precision 0)
- * and their final records written to d_particles.  Scratch: at least
+ * steps recomputed once.  Particles are tracked as by cct_track with the
+ * same precision (0 = FP64 with d_kls/d_p0s, 1 = FP32-compensated with
+ * d_packed; the adjoint sweeps run in that precision) and their final records
+ * are written to d_particles.  Scratch: at least
  * cct_adjoint_scratch_bytes(n_designs, n_particles, steps, checkpoint_steps)
  * bytes, `steps` an upper bound of any particle's step count.  Synchronous. */
 int64_t cct_adjoint_scratch_bytes(int32_t n_designs, int64_t n_particles,
                                   int32_t max_steps, int32_t checkpoint_steps);
 int cct_track_adjoint(const double *d_kls, const double *d_p0s,
-                      const int64_t *d_seg_off, const double *d_qs,
-                      const int64_t *d_qs_off, int32_t n_designs,
-                      double *d_particles, int64_t n_particles, double distance,
-                      double footstep, const double *d_exit_frame, double *d_J,
+                      const int64_t *d_seg_off, const void *d_packed,
+                      const double *d_qs, const int64_t *d_qs_off,
+                      int32_t n_designs, double *d_particles,
+                      int64_t n_particles, double distance, double footstep,
+                      int32_t precision, const double *d_exit_frame, double *d_J,
                       double *d_seg_grad, int32_t checkpoint_steps,
                       void *d_scratch, int64_t scratch_bytes, void *stream);
 

@@ -142,3 +142,18 @@ def test_autograd_function_and_batched_designs():
     # each design's gradient equals the one of a single-design run
     _, g0 = design_gradients([GantryDesign(theta[0].detach().numpy(), part_per_winding=60)], ps, 0.1, 0.01, 215.0)
     np.testing.assert_allclose(g2[0], g0[0], rtol=1e-12, atol=0)
+
+
+def test_f32c_adjoint_matches_f64_adjoint_and_differences():
+    kw = W.design_population(1, seed=3)[0]
+    theta = np.array(kw["dicct345_tilt_angles"] + kw["agcct345_tilt_angles"]
+                     + [kw["dicct345_current"], kw["dicct345_current"], kw["agcct345_current"],
+                        kw["agcct345_current"], 0.95])
+    base = GantryDesign(theta, part_per_winding=60)
+    ps = W.beam_particles(base.beamline, 96, seed=7, kinetic_MeV=215.0)   # 96: blocks of 64, a ragged one
+    L, step = 0.3, 0.01
+    J64, g64 = design_gradients([base], ps, L, step, 215.0, checkpoint=8, precision="f64")
+    J32, g32 = design_gradients([base], ps, L, step, 215.0, checkpoint=8, precision="f32c")
+    assert abs(J32[0] - J64[0]) <= 1e-6 * J64[0]
+    scale = np.abs(g64[0]).max()
+    assert np.all(np.abs(g32[0] - g64[0]) <= 1e-4 * np.abs(g64[0]) + 1e-6 * scale), (g32, g64)
