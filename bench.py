@@ -198,12 +198,13 @@ def measure_design_grads(args, rank):
     """design-grads/s: 13-parameter gradients of J = <x^2> + <y^2> at the exit for 16 gantry
     designs x 1024 protons in one adjoint run, on a slice of RK4 steps (1 mm):
     FP32c (forward and adjoint sweeps in packed FP32 with compensation) on args.adjoint_steps
-    steps, the FP64 adjoint on 1/16 of them.  GPU time (cct_track_adjoint: forward with
-    checkpoints, recompute, reverse sweeps, segment gradients) and host time (segment-
-    generation Jacobian by complex step, 13-parameter mapping) are reported apart."""
+    steps, the FP64 adjoint on 1/16 of them.  Timed apart: the design set (segments generated
+    on the GPU from layer records), the adjoint (cct_track_adjoint: forward with checkpoints,
+    recompute, reverse sweeps, segment gradients) and the parameter Jacobian (forward-mode
+    contraction on the GPU, cct_segments_param_grad, plus the 13-parameter grouping)."""
     import torch
     from cctpy_gb300 import engine, workloads as W
-    from cctpy_gb300.adjoint import GantryDesign, exit_frame, layer_gradients, segment_gradient
+    from cctpy_gb300.adjoint import GantryDesign, exit_frame, layer_grads_from_rows, segment_gradient
 
     kws = W.design_population(16, seed=3)
     thetas = [np.array(kw["dicct345_tilt_angles"] + kw["agcct345_tilt_angles"]
@@ -211,36 +212,40 @@ def measure_design_grads(args, rank):
                           kw["agcct345_current"], 0.95]) for kw in kws]
     designs = [GantryDesign(t, part_per_winding=360) for t in thetas]
     ps = W.beam_particles(designs[0].beamline, 1024, seed=4 + rank, kinetic_MeV=215.0)
+    engine.design_set_of([designs[0].beamline], segments="device")          # warm-up
+    torch.cuda.synchronize()
     t0 = time.perf_counter()
-    ds = engine.design_set_of([d.beamline for d in designs])
+    ds = engine.design_set_of([d.beamline for d in designs], segments="device")
     ds.packed()
+    torch.cuda.synchronize()
     t_setup = time.perf_counter() - t0
     n_seg = ds.n_segments
     out = {"workload": f"16 second-section designs ({n_seg} segments total), 1024 protons each, 13 parameters "
                        "(8 tilts, 4 layer currents, winding radius), J = <x^2>+<y^2> at the exit; "
                        "checkpoints every 16 steps",
-           "host_design_set_seconds": t_setup}
+           "design_set_seconds": t_setup}
     for prec, steps in (("f32c", args.adjoint_steps), ("f64", max(1, args.adjoint_steps // 16))):
         L = steps * 0.001
         frames = np.tile(exit_frame(designs[0].beamline.trajectory, L, 215.0), (16, 1))
         segment_gradient(ds, ps, 0.002, 0.001, frames, 16, prec)          # warm-up
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        J, seg, _ = segment_gradient(ds, ps, L, 0.001, frames, 16, prec)
+        J, seg, _ = segment_gradient(ds, ps, L, 0.001, frames, 16, prec, on_device=True)
         torch.cuda.synchronize()
         t_gpu = time.perf_counter() - t0
         t0 = time.perf_counter()
-        g = [d.gradient(layer_gradients(d.beamline.magnets, seg[int(ds.h_seg_off[i]):int(ds.h_seg_off[i + 1])]))
+        rows = ds.param_grad(seg)
+        g = [d.gradient(layer_grads_from_rows(d.beamline.magnets, rows[ds.layer_design == i]))
              for i, d in enumerate(designs)]
-        t_host = time.perf_counter() - t0
+        t_jac = time.perf_counter() - t0
         fwd_pairs = 1024 * steps * 4 * n_seg
-        out[prec] = {"steps": steps, "gpu_seconds": t_gpu, "host_mapping_seconds": t_host,
-                     "design_grads_per_s": 16 / (t_gpu + t_host),
-                     "design_grad_steps_per_s": 16 * steps / (t_gpu + t_host),
-                     "design_grad_steps_per_s_gpu": 16 * steps / t_gpu,
-                     "forward_equivalent_gpairs_per_s_gpu": fwd_pairs / t_gpu / 1e9,
+        out[prec] = {"steps": steps, "adjoint_seconds": t_gpu, "jacobian_seconds": t_jac,
+                     "design_grads_per_s": 16 / (t_gpu + t_jac),
+                     "design_grad_steps_per_s": 16 * steps / (t_gpu + t_jac),
+                     "design_grad_steps_per_s_adjoint": 16 * steps / t_gpu,
+                     "forward_equivalent_gpairs_per_s": fwd_pairs / t_gpu / 1e9,
                      "gradient_norm_design0": float(np.linalg.norm(g[0]))}
-    out["speedup_f32c_vs_f64_gpu"] = out["f32c"]["design_grad_steps_per_s_gpu"] / out["f64"]["design_grad_steps_per_s_gpu"]
+    out["speedup_f32c_vs_f64"] = out["f32c"]["design_grad_steps_per_s"] / out["f64"]["design_grad_steps_per_s"]
     return out
 
 

@@ -7,10 +7,12 @@ The GPU (libcctgpu ``cct_track_adjoint``) returns, for every design, the objecti
 -- the RMS spot size squared plus the centroid squared in both planes -- and its gradient
 with respect to every current element (kl_i, p0_i), by the discrete adjoint of the FP64
 RK4 track with checkpointing.  This module maps those segment gradients to design
-parameters through the Jacobian of segment generation (``CCT.path_local``), taken by the
-complex-step method: the winding path is evaluated once per parameter with that parameter
-perturbed by i*1e-30, which gives the exact derivative to rounding with no subtractive
-cancellation.  The magnet frames are held fixed (they come from the design orbit).
+parameters through the Jacobian of segment generation (``CCT.path_local``): on the GPU by
+forward-mode derivatives of the generation formulas (``cct_segments_param_grad``, the
+default), or on the host by the complex-step method (the winding path evaluated once per
+parameter with that parameter perturbed by i*1e-30, exact to rounding with no subtractive
+cancellation), which the tests use as the check.  The magnet frames are held fixed (they
+come from the design orbit).
 
 Per CCT layer the parameters are its tilt angles (degrees), its current and its winding
 torus radius big_r.  ``GantryDesign`` groups the layers of the HUST second bending section
@@ -52,9 +54,10 @@ def objective_host(final: np.ndarray, frame: np.ndarray) -> float:
 
 
 def segment_gradient(ds: engine.DesignSet, particles, distance: float, footstep: float, frames: np.ndarray,
-                     checkpoint: int = 64, precision: str = "f64"):
+                     checkpoint: int = 64, precision: str = "f64", on_device: bool = False):
     """(J (D,), dJ/d(kl, p0) (N_seg, 6), final records (D, n, 10)) for the designs of `ds`;
-    precision "f64" or "f32c" (forward and adjoint sweeps)."""
+    precision "f64" or "f32c" (forward and adjoint sweeps).  on_device=True returns the
+    segment gradient as a CUDA tensor (for DesignSet.param_grad)."""
     lib = _lib.load()
     dev = ds.kls.device
     p = torch.as_tensor(np.asarray(particles, dtype=np.float64), device=dev)
@@ -81,7 +84,8 @@ def segment_gradient(ds: engine.DesignSet, particles, distance: float, footstep:
                                float(distance), float(footstep), prec, fr.data_ptr(), J.data_ptr(), grad.data_ptr(),
                                int(checkpoint), sc.data_ptr(), int(nbytes), engine._stream())
     _lib.check(rc, "cct_track_adjoint")
-    return J.cpu().numpy(), grad[:ds.n_segments].cpu().numpy(), p.cpu().numpy()
+    g = grad[:ds.n_segments]
+    return J.cpu().numpy(), (g if on_device else g.cpu().numpy()), p.cpu().numpy()
 
 
 # ---------------------------------------------------------------- segment-generation Jacobian
@@ -194,16 +198,42 @@ class GantryDesign:
         return g
 
 
+def layer_grads_from_rows(magnets: Sequence, rows: np.ndarray) -> List[Dict[str, object]]:
+    """Per-magnet gradient dicts (None for QS and zero-current layers) from the rows of
+    DesignSet.param_grad, which follow engine.device_layers' layer order."""
+    out, k = [], 0
+    for m in magnets:
+        if engine._classify(m) != "cct" or abs(float(m.current)) <= 1e-6:
+            out.append(None)
+            continue
+        r = rows[k]
+        k += 1
+        out.append({"tilt": [float(v) for v in r[:len(m.tilt_angles)]], "current": float(r[8]),
+                    "big_r": float(r[9])})
+    return out
+
+
 def design_gradients(designs: Sequence[GantryDesign], particles: np.ndarray, distance: float, footstep: float,
-                     kinetic_MeV: float, checkpoint: int = 64, precision: str = "f64") -> Tuple[np.ndarray, np.ndarray]:
+                     kinetic_MeV: float, checkpoint: int = 64, precision: str = "f64",
+                     jacobian: str = "device") -> Tuple[np.ndarray, np.ndarray]:
     """J (D,) and dJ/dtheta (D, 13) of every design, all tracked in one adjoint run.  The
     designs share the design orbit: particles start at s = 0 and the objective is read in
-    the ideal particle's frame at s = distance."""
-    ds = engine.design_set_of([d.beamline for d in designs])
+    the ideal particle's frame at s = distance.  jacobian="device" generates the segments
+    and contracts the segment gradient with the segment-generation Jacobian on the GPU
+    (forward mode, cct_segments_param_grad); "host" builds segments with numpy and takes
+    the Jacobian by complex step."""
+    if jacobian not in ("device", "host"):
+        raise ValueError(f"jacobian must be 'device' or 'host', not {jacobian!r}")
+    ds = engine.design_set_of([d.beamline for d in designs], segments=jacobian)
     frame = exit_frame(designs[0].beamline.trajectory, distance, kinetic_MeV)
     J, seg, _ = segment_gradient(ds, particles, distance, footstep, np.tile(frame, (len(designs), 1)), checkpoint,
-                                 precision)
+                                 precision, on_device=(jacobian == "device"))
     grads = np.zeros((len(designs), 13))
+    if jacobian == "device":
+        rows = ds.param_grad(seg)
+        for d, des in enumerate(designs):
+            grads[d] = des.gradient(layer_grads_from_rows(des.beamline.magnets, rows[ds.layer_design == d]))
+        return J, grads
     for d, des in enumerate(designs):
         a, b = int(ds.h_seg_off[d]), int(ds.h_seg_off[d + 1])
         grads[d] = des.gradient(layer_gradients(des.beamline.magnets, seg[a:b]))

@@ -74,6 +74,45 @@ def qs_record(m) -> np.ndarray:
     return np.asarray(m.to_numpy_array(np.float64), dtype=np.float64)
 
 
+LAYER_DOUBLES, LAYER_MAX_TILTS, LAYER_PARAMS = 32, 8, 10
+
+
+def _xyz(p) -> List[float]:
+    return [float(p.x), float(p.y), float(p.z)]
+
+
+def layer_record(m) -> np.ndarray:
+    """The 32-double layer record of a CCT (ours or cctpy's) that cct_segments_build reads:
+    frame (origin, XI, YI, ZI), big_r, small_r, current, xi/phi start and end, winding number,
+    segments per winding, tilt count and tilt angles (degrees)."""
+    lcs = m.local_coordinate_system
+    tilts = [float(t) for t in m.tilt_angles]
+    if len(tilts) > LAYER_MAX_TILTS:
+        raise ValueError(f"{len(tilts)} tilt angles; the device generator takes at most {LAYER_MAX_TILTS}")
+    s, e = m.starting_point_in_ksi_phi_coordinate, m.end_point_in_ksi_phi_coordinate
+    r = np.zeros(LAYER_DOUBLES)
+    r[0:12] = _xyz(lcs.location) + _xyz(lcs.XI) + _xyz(lcs.YI) + _xyz(lcs.ZI)
+    r[12:22] = [m.big_r, m.small_r, m.current, s.x, s.y, e.x, e.y, m.winding_number,
+                m.disperse_number_per_winding, len(tilts)]
+    r[22:22 + len(tilts)] = tilts
+    return r
+
+
+def device_layers(magnets: Sequence) -> tuple:
+    """(layer records, CCT magnets, QS records (m, 16)) of one design, with the CCT layers in
+    host_design's order (zero-current layers dropped)."""
+    recs, ccts, qss = [], [], []
+    for m in magnets:
+        if _classify(m) == "cct":
+            if abs(float(m.current)) <= 1e-6:
+                continue
+            recs.append(layer_record(m))
+            ccts.append(m)
+        else:
+            qss.append(qs_record(m))
+    return recs, ccts, (np.stack(qss) if qss else np.zeros((0, 16)))
+
+
 def host_design(magnets: Sequence) -> tuple:
     """(kls (N,3), p0s (N,3), qs (M,16)) of one design.  A CCT with |current| <= 1e-6
     contributes nothing (cct.py:254-255)."""
@@ -95,27 +134,74 @@ def host_design(magnets: Sequence) -> tuple:
 
 
 class DesignSet:
-    """Several designs resident in HBM: segments (FP64), QS records, CSR offsets."""
+    """Several designs resident in HBM: segments (FP64), QS records, CSR offsets.
+
+    Built from host segment arrays (`designs`: per design (kls, p0s, qs)) or, with
+    `DesignSet.from_layers`, from CCT layer records with the segments generated on the
+    device (cct_segments_build); the latter keeps the records (`layers`, `h_layers`) and
+    each layer's design (`layer_design`) for the parameter Jacobian."""
 
     def __init__(self, designs: Sequence[tuple]):
+        seg_counts = [d[0].shape[0] for d in designs]
+        cat = lambda k, w: np.concatenate([d[k] for d in designs]) if designs else np.zeros((0, w))
         dev = _device()
-        self.n_designs = len(designs)
+        self._finish(seg_counts, [d[2] for d in designs], torch.from_numpy(cat(0, 3)).to(dev),
+                     torch.from_numpy(cat(1, 3)).to(dev))
+
+    def _finish(self, seg_counts, qs_list, kls, p0s):
+        dev = kls.device
+        self.n_designs = len(seg_counts)
         if self.n_designs == 0:
             raise ValueError("empty design set")
-        seg_off = np.zeros(self.n_designs + 1, dtype=np.int64)
-        qs_off = np.zeros(self.n_designs + 1, dtype=np.int64)
-        for i, (kl, _, qs) in enumerate(designs):
-            seg_off[i + 1] = seg_off[i] + kl.shape[0]
-            qs_off[i + 1] = qs_off[i] + qs.shape[0]
-        self.h_seg_off = seg_off
-        self.h_qs_off = qs_off
-        cat = lambda k, w: np.concatenate([d[k] for d in designs]) if designs else np.zeros((0, w))
-        self.kls = torch.from_numpy(cat(0, 3)).to(dev)
-        self.p0s = torch.from_numpy(cat(1, 3)).to(dev)
-        self.qs = torch.from_numpy(cat(2, 16)).to(dev)
-        self.seg_off = torch.from_numpy(seg_off).to(dev)
-        self.qs_off = torch.from_numpy(qs_off).to(dev)
+        self.h_seg_off = np.concatenate([[0], np.cumsum(seg_counts)]).astype(np.int64)
+        self.h_qs_off = np.concatenate([[0], np.cumsum([q.shape[0] for q in qs_list])]).astype(np.int64)
+        self.kls, self.p0s = kls, p0s
+        qs = np.concatenate(qs_list) if qs_list else np.zeros((0, 16))
+        self.qs = torch.from_numpy(np.ascontiguousarray(qs, dtype=np.float64).reshape(-1, 16)).to(dev)
+        self.seg_off = torch.from_numpy(self.h_seg_off).to(dev)
+        self.qs_off = torch.from_numpy(self.h_qs_off).to(dev)
         self._packed = None
+        if not hasattr(self, "layers"):
+            self.layers = self.h_layers = self.layer_design = None
+
+    @classmethod
+    def from_layers(cls, layer_lists: Sequence[Sequence[np.ndarray]], qs_lists: Sequence[np.ndarray]) -> "DesignSet":
+        """Design set whose segments are generated on the device from CCT layer records
+        (`layer_record`): layer_lists[d] = records of design d, qs_lists[d] = (m, 16)."""
+        lib = _lib.load()
+        dev = _device()
+        self = cls.__new__(cls)
+        recs = [r for ls in layer_lists for r in ls]
+        self.h_layers = np.ascontiguousarray(np.stack(recs) if recs else np.zeros((0, LAYER_DOUBLES)))
+        self.layer_design = np.array([d for d, ls in enumerate(layer_lists) for _ in ls], dtype=np.int64)
+        counts = [int(r[19]) * int(r[20]) for r in recs]
+        seg_counts = [sum(counts[i] for i in np.nonzero(self.layer_design == d)[0]) for d in range(len(layer_lists))]
+        n = int(sum(counts))
+        if recs:
+            total = lib.cct_layer_segments(self.h_layers.ctypes.data_as(ctypes.c_void_p), len(recs))
+            _lib.check(0 if total >= 0 else _lib.CCT_ERR_ARG, "cct_layer_segments")
+        kls = torch.empty((n, 3), dtype=torch.float64, device=dev)
+        p0s = torch.empty((n, 3), dtype=torch.float64, device=dev)
+        self.layers = torch.from_numpy(self.h_layers).to(dev)
+        if recs:
+            _lib.check(lib.cct_segments_build(_ptr(self.layers), len(recs), _ptr(kls), _ptr(p0s), n, _stream()),
+                       "cct_segments_build")
+        self._finish(seg_counts, [np.asarray(q, dtype=np.float64).reshape(-1, 16) for q in qs_lists], kls, p0s)
+        return self
+
+    def param_grad(self, seg_grad: torch.Tensor) -> np.ndarray:
+        """(n_layers, 10) dJ/d(tilt 0..7 [deg], current [A], big_r [m]) of every layer from a
+        device segment gradient (n_segments, 6) (cct_segments_param_grad)."""
+        if self.layers is None:
+            raise ValueError("param_grad needs a design set built from layer records (DesignSet.from_layers)")
+        lib = _lib.load()
+        g = seg_grad.to(dtype=torch.float64).contiguous()
+        if g.shape != (self.n_segments, 6) or not g.is_cuda:
+            raise ValueError(f"segment gradient must be a CUDA (n_segments, 6) tensor, not {tuple(g.shape)}")
+        out = torch.empty((self.h_layers.shape[0], LAYER_PARAMS), dtype=torch.float64, device=g.device)
+        _lib.check(lib.cct_segments_param_grad(_ptr(self.layers), self.h_layers.shape[0], _ptr(g), self.n_segments,
+                                               _ptr(out), _stream()), "cct_segments_param_grad")
+        return out.cpu().numpy()
 
     @property
     def n_segments(self) -> int:
@@ -153,8 +239,17 @@ def design_of(obj) -> DesignSet:
     return ds
 
 
-def design_set_of(objs: Sequence) -> DesignSet:
-    return DesignSet([host_design(magnet_list(o)) for o in objs])
+def design_set_of(objs: Sequence, segments: str = "host") -> DesignSet:
+    """Design set of several beamlines / magnets.  segments="host" builds the segment arrays
+    with numpy and copies them; "device" generates them on the GPU from layer records."""
+    if segments == "host":
+        return DesignSet([host_design(magnet_list(o)) for o in objs])
+    if segments != "device":
+        raise ValueError(f"segments must be 'host' or 'device', not {segments!r}")
+    parts = [device_layers(magnet_list(o)) for o in objs]
+    ds = DesignSet.from_layers([p[0] for p in parts], [p[2] for p in parts])
+    ds.layer_magnets = [m for p in parts for m in p[1]]
+    return ds
 
 
 def field_at_points(ds: DesignSet, points, precision: str = "f64", design: int = 0, out_host=None):

@@ -173,6 +173,49 @@ int cct_track_static_scratch(const double *d_kls, const double *d_p0s,
                              int64_t n_particles, double distance, double footstep,
                              int32_t precision, void *stream);
 
+/* ---------------------------------------------------------------------------
+ * Device-side segment generation.  Replaces the host loop of the CCT
+ * constructor and its global export (cct.py:87-164 with phi_ksi_function
+ * :166-188 and BipolarToroidalCoordinateSystem.convert :213-224; export
+ * :423-457), which the reference runs in Python for every design on every GPU
+ * call.  A layer is described by one record of CCT_LAYER_DOUBLES doubles:
+ *   [0..2]  origin, [3..5] XI, [6..8] YI, [9..11] ZI of its local frame
+ *   [12] big_r  [13] small_r  [14] current (A)
+ *   [15] xi start  [16] phi start  [17] xi end  [18] phi end
+ *        (starting/end_point_in_ksi_phi_coordinate)
+ *   [19] winding number  [20] segments per winding
+ *   [21] number of tilt angles (0..CCT_LAYER_MAX_TILTS)
+ *   [22..29] tilt angles in degrees  [30..31] unused (0)
+ * Layer l owns winding_number * segments_per_winding segments, the layers'
+ * segments concatenated in record order (a design set lists its designs'
+ * layers one design after the other, as cct_track's segment offsets expect).
+ * Values agree with the host construction to rounding of the trigonometric
+ * functions (about 1e-13 relative in kl).  Both calls read the records back to
+ * check them (CCT_ERR_ARG on a bad record or a segment count other than
+ * n_seg) and are synchronous.
+ * ------------------------------------------------------------------------- */
+#define CCT_LAYER_DOUBLES 32
+#define CCT_LAYER_MAX_TILTS 8
+#define CCT_LAYER_PARAMS 10
+
+/* Total segment count of host layer records (-1 and an error on a bad record). */
+int64_t cct_layer_segments(const double *h_layers, int32_t n_layers);
+
+/* Writes d_kls[n_seg*3], d_p0s[n_seg*3] (global frame, FP64) of the layers in
+ * d_layers[n_layers*CCT_LAYER_DOUBLES]. */
+int cct_segments_build(const double *d_layers, int32_t n_layers, double *d_kls,
+                       double *d_p0s, int64_t n_seg, void *stream);
+
+/* Maps a segment gradient d_seg_grad[n_seg*6] (dJ/dkl, dJ/dp0 as written by
+ * cct_track_adjoint) to d_param_grad[n_layers*CCT_LAYER_PARAMS] =
+ * dJ/d(tilt angle 0..7 [per degree], current [per A], big_r [per m]) of every
+ * layer (tilts past the layer's count are 0), by forward-mode derivatives of
+ * the segment construction; the frame, small_r and xi/phi ends are held fixed.
+ * No counterpart in the reference (it has no derivatives). */
+int cct_segments_param_grad(const double *d_layers, int32_t n_layers,
+                            const double *d_seg_grad, int64_t n_seg,
+                            double *d_param_grad, void *stream);
+
 /* Measures the device's fused multiply-add pipe peak (flop/s, 2 per FMA) with
  * independent FMA chains on every SM: kind 0 = scalar FP32, 1 = FP64, 2 = packed
  * FP32x2.  These are the roofline denominators of the field kernels.

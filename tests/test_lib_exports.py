@@ -48,3 +48,18 @@ def test_host_only_calls(lib):
     assert "negative" in _lib.last_error()
     bad = (ctypes.c_int64 * 2)(10, 5)
     assert lib.cct_f32c_packed_bytes(ctypes.cast(bad, ctypes.c_void_p), 1) == -1
+
+
+def test_layer_records_checked_on_host(lib):
+    import numpy as np
+    from cctpy_gb300 import engine, workloads as W
+    _, dipole = W.build_single_dipole()
+    rec = np.ascontiguousarray(np.stack([engine.layer_record(dipole)] * 2))
+    assert lib.cct_layer_segments(rec.ctypes.data_as(ctypes.c_void_p), 2) == 2 * 46080
+    bad = rec.copy()
+    bad[1, 21] = 9                      # more tilt angles than a record holds
+    assert lib.cct_layer_segments(bad.ctypes.data_as(ctypes.c_void_p), 2) == -1
+    assert "layer 1" in _lib.last_error()
+    bad = rec.copy()
+    bad[0, 19] = 2.5                    # fractional winding number
+    assert lib.cct_layer_segments(bad.ctypes.data_as(ctypes.c_void_p), 2) == -1
