@@ -235,10 +235,7 @@ __global__ void __launch_bounds__(kTrackBlock) adjoint_kernel(AdjParams A) {
     const int64_t n_units = P.unit_off[P.n_designs];
     const int64_t first = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (A.step_end <= A.step_begin) return;
-    if (threadIdx.x == 0) {
-        for (int s = 0; s < kRing; ++s) cctdev::mbar_init(&sm.full[s], 1);
-        cctdev::mbar_fence_init();
-    }
+    if (threadIdx.x == 0) ring_init(sm);
     for (int64_t pi = first; pi < total; pi += tstride) begin_step(A, pi, A.step_end - 1);
     if (!grid_barrier(P, sm)) return;
     uint32_t kt = 0;   // tiles consumed through the TMA ring by this CTA (FP32c)

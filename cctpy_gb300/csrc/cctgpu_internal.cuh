@@ -112,4 +112,23 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity
     return false;
 }
 
+// Release of a ring slot without a CTA-wide barrier.  Every warp of the CTA calls this (all
+// lanes, converged) after its last read of the slot; lane 0 of the last of `n_warps` warps
+// to arrive gets true and refills the slot.  The counter's fences order every warp's shared
+// reads of the slot before the refill (the refilling lane then issues fence.proxy.async
+// before the bulk copy); the counter is reset for the slot's next round.
+__device__ __forceinline__ bool ring_release_last(int *cnt, int n_warps) {
+    __syncwarp();
+    bool last = false;
+    if ((threadIdx.x & 31) == 0) {
+        __threadfence_block();
+        last = atomicAdd(cnt, 1) == n_warps - 1;
+        if (last) {
+            __threadfence_block();
+            atomicExch(cnt, 0);
+        }
+    }
+    return last;
+}
+
 }  // namespace cctdev

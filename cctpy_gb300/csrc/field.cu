@@ -219,20 +219,25 @@ int launch_pack_f32c(const double *kls, const double *p0s, const int64_t *h_seg_
 }
 
 // ===================================================================== FP32c field
-constexpr int kF32Block = 256;
+constexpr int kF32Block = 128;   // 4 CTAs per SM: measured faster than 2 x 256 on GB300
 constexpr int kF32Ppt = 2;
+constexpr int kF32Blocks = 4;
+constexpr int kF32Unroll = 2;
 constexpr int kStages = 4;
 constexpr uint32_t kWaitPolls = 1u << 22;
 
 __device__ int g_field_status;   // last non-OK status seen by a field kernel (sticky)
 
-__global__ void __launch_bounds__(kF32Block, 2) field_f32c_kernel(const unsigned char *__restrict__ packed,
+__global__ void __launch_bounds__(kF32Block, kF32Blocks) field_f32c_kernel(const unsigned char *__restrict__ packed,
                                                                   int design, const double *__restrict__ qs,
                                                                   int n_qs, const double *__restrict__ pts,
                                                                   int64_t n, double *__restrict__ B) {
     __shared__ __align__(128) unsigned char buf[kStages][kTileBytes];
     __shared__ __align__(8) uint64_t full[kStages];
-    const int tid = threadIdx.x;
+    __shared__ int64_t last_issued[kStages];   // tile index last copied into each slot (-1: none)
+    __shared__ int released[kStages];          // warps done with the slot's current tile
+    constexpr int kWarps = kF32Block / 32;
+    const int tid = threadIdx.x, lane = tid & 31;
     const int64_t magic = reinterpret_cast<const int64_t *>(packed)[0];
     const int64_t n_designs = reinterpret_cast<const int64_t *>(packed)[1];
     const int64_t base = (int64_t)blockIdx.x * kF32Block * kF32Ppt;
@@ -250,12 +255,17 @@ __global__ void __launch_bounds__(kF32Block, 2) field_f32c_kernel(const unsigned
     const int64_t nt = tile_off[design + 1] - tile_off[design];
 
     if (tid == 0) {
-        for (int s = 0; s < kStages; ++s) cctdev::mbar_init(&full[s], 1);
+        for (int s = 0; s < kStages; ++s) {
+            cctdev::mbar_init(&full[s], 1);
+            released[s] = 0;
+            last_issued[s] = -1;
+        }
         cctdev::mbar_fence_init();
     }
     __syncthreads();
     if (tid == 0) {
         for (int s = 0; s < kStages && s < nt; ++s) {
+            last_issued[s] = s;
             cctdev::mbar_arrive_expect_tx(&full[s], kTileBytes);
             cctdev::bulk_g2s(buf[s], tiles + (int64_t)s * kTileBytes, kTileBytes, &full[s]);
         }
@@ -272,30 +282,34 @@ __global__ void __launch_bounds__(kF32Block, 2) field_f32c_kernel(const unsigned
     F32cAcc<kF32Ppt> acc;
     acc.zero();
 
+    // Warps run through the ring independently: a warp waits only for its next tile to land;
+    // the last warp done with a slot refills it with the tile kStages further on.
     bool failed = false;
     for (int64_t t = 0; t < nt; ++t) {
         const int s = (int)(t % kStages);
         const bool ok = cctdev::mbar_wait_bounded(&full[s], (uint32_t)((t / kStages) & 1), kWaitPolls);
-        // also orders: every thread has finished tile t-1 before its buffer is refilled
-        if (__syncthreads_or(!ok)) {
+        if (!__all_sync(0xffffffffu, ok)) {
             failed = true;
             break;
         }
-        if (tid == 0 && t >= 1 && t - 1 + kStages < nt) {
-            const int sp = (int)((t - 1) % kStages);
+        tile_f32c<kF32Ppt, kF32Unroll>(buf[s], ph, pl, acc);
+        if (cctdev::ring_release_last(&released[s], kWarps) && t + kStages < nt) {
+            last_issued[s] = t + kStages;
             cctdev::fence_proxy_async();
-            cctdev::mbar_arrive_expect_tx(&full[sp], kTileBytes);
-            cctdev::bulk_g2s(buf[sp], tiles + (t - 1 + kStages) * (int64_t)kTileBytes, kTileBytes, &full[sp]);
-        }
-        tile_f32c<kF32Ppt>(buf[s], ph, pl, acc);
-    }
-    if (failed) {
-        // let copies still in flight land before the CTA's shared memory is released
-        if (tid == 0) {
-            for (int s = 0; s < kStages; ++s) (void)cctdev::mbar_wait_bounded(&full[s], 0, 1024);
-            atomicExch(&g_field_status, (int)CCT_ERR_TIMEOUT);
+            cctdev::mbar_arrive_expect_tx(&full[s], kTileBytes);
+            cctdev::bulk_g2s(buf[s], tiles + (t + kStages) * (int64_t)kTileBytes, kTileBytes, &full[s]);
         }
     }
+    failed = __syncthreads_or(failed);
+    if (failed && tid == 0) {
+        // a warp gave up: let the last copy into every slot land before the CTA's shared
+        // memory is released (earlier copies into a slot were consumed before its refill)
+        for (int s = 0; s < kStages; ++s)
+            if (last_issued[s] >= 0)
+                (void)cctdev::mbar_wait_bounded(&full[s], (uint32_t)((last_issued[s] / kStages) & 1), kWaitPolls);
+        atomicExch(&g_field_status, (int)CCT_ERR_TIMEOUT);
+    }
+    (void)lane;
 
 #pragma unroll
     for (int i = 0; i < kF32Ppt; ++i) {

@@ -76,8 +76,9 @@ struct F32cAcc {
 };
 
 // Accumulate segments [4*g0, 4*g1) of one tile (default: all 128) for PPT points given as
-// double-float (hi, lo) coordinates.
-template <int PPT>
+// double-float (hi, lo) coordinates.  JU: unroll of the 4-segment loop (2 keeps more
+// independent pair terms in flight where registers allow).
+template <int PPT, int JU = 1>
 __device__ __forceinline__ void tile_f32c(const unsigned char *tile, const float (&ph)[PPT][3],
                                           const float (&pl)[PPT][3], F32cAcc<PPT> &acc, int g0 = 0,
                                           int g1 = kTile / 4) {
@@ -98,7 +99,7 @@ __device__ __forceinline__ void tile_f32c(const unsigned char *tile, const float
         f2 B[PPT][3];
 #pragma unroll
         for (int i = 0; i < PPT; ++i) B[i][0] = B[i][1] = B[i][2] = 0ull;
-#pragma unroll 1
+#pragma unroll JU
         for (int j = sb; j < se; ++j) {                          // 4 segments per iteration
             const ulonglong2 KX = v[0 * Q + j], KY = v[1 * Q + j], KZ = v[2 * Q + j];
             const ulonglong2 NX = v[3 * Q + j], NY = v[4 * Q + j], NZ = v[5 * Q + j];

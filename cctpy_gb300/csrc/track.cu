@@ -31,10 +31,7 @@ __global__ void __launch_bounds__(kTrackBlock) track_kernel(TrackParams P) {
     __shared__ __align__(128) TrackSmem sm;
     const int64_t total = (int64_t)P.n_designs * P.n_p;
     const int64_t tstride = (int64_t)gridDim.x * blockDim.x;
-    if (threadIdx.x == 0) {
-        for (int s = 0; s < kRing; ++s) cctdev::mbar_init(&sm.full[s], 1);
-        cctdev::mbar_fence_init();
-    }
+    if (threadIdx.x == 0) ring_init(sm);
     uint32_t kt = 0;   // tiles consumed through the ring by this CTA
 
     // init: state from the particle records; step count and dt as the CPU reference computes them

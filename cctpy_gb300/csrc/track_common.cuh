@@ -59,9 +59,22 @@ constexpr int kRec = 12;
 struct TrackSmem {
     unsigned char ring[kRing][kTileBytes];
     uint64_t full[kRing];
+    uint32_t last_issued[kRing];   // ring tile index last copied into each slot (kNone: none)
+    int released[kRing];           // warps done with the slot's current tile
     double red[kRedDoubles];
     int verdict;
 };
+constexpr uint32_t kNone = 0xffffffffu;
+
+// Ring set-up by thread 0 at kernel start (made visible by the kernel's first barrier).
+static __device__ __forceinline__ void ring_init(TrackSmem &sm) {
+    for (int s = 0; s < kRing; ++s) {
+        cctdev::mbar_init(&sm.full[s], 1);
+        sm.last_issued[s] = kNone;
+        sm.released[s] = 0;
+    }
+    cctdev::mbar_fence_init();
+}
 
 __device__ __forceinline__ unsigned long long global_ns() {
     unsigned long long t;
@@ -232,36 +245,43 @@ static __device__ bool unit_sum_f32c(const TrackParams &P, const PointSrc &src, 
 
     const unsigned char *tiles = P.tiles + (P.tile_off[U.d] + U.t_beg) * (int64_t)kTileBytes;
     const int64_t nt = U.t_end - U.t_beg;
-    if (tid == 0) {
+    if (tid == 0) {   // the ring is idle here: the previous unit ended at a CTA barrier
         for (int64_t t = 0; t < kRing && t < nt; ++t) {
             const int s = (int)((kt + t) % kRing);
+            sm.last_issued[s] = kt + (uint32_t)t;
             cctdev::fence_proxy_async();
             cctdev::mbar_arrive_expect_tx(&sm.full[s], kTileBytes);
             cctdev::bulk_g2s(sm.ring[s], tiles + t * (int64_t)kTileBytes, kTileBytes, &sm.full[s]);
         }
     }
+    // Warps run through the ring independently: a warp waits only for its next tile to
+    // land; the last warp done with a slot refills it with the tile kRing further on.
     bool ok_all = true;
     for (int64_t t = 0; t < nt; ++t) {
         const uint32_t k = kt + (uint32_t)t;
         const int s = (int)(k % kRing);
         const bool ok = cctdev::mbar_wait_bounded(&sm.full[s], (k / kRing) & 1u, kTmaPolls);
-        if (__syncthreads_or(!ok)) {   // also: all threads are done with tile t-1
+        if (!__all_sync(0xffffffffu, ok)) {
             ok_all = false;
             break;
         }
-        if (tid == 0 && t >= 1 && t - 1 + kRing < nt) {
-            const int sp = (int)((k - 1) % kRing);
-            cctdev::fence_proxy_async();
-            cctdev::mbar_arrive_expect_tx(&sm.full[sp], kTileBytes);
-            cctdev::bulk_g2s(sm.ring[sp], tiles + (t - 1 + kRing) * (int64_t)kTileBytes, kTileBytes, &sm.full[sp]);
-        }
         if (GRAD) tile_grad_f32c<PPT>(sm.ring[s], ph, pl, a, acc, g0, g1);
         else tile_f32c<PPT>(sm.ring[s], ph, pl, acc, g0, g1);
+        if (cctdev::ring_release_last(&sm.released[s], kTrackWarps) && t + kRing < nt) {
+            sm.last_issued[s] = k + kRing;
+            cctdev::fence_proxy_async();
+            cctdev::mbar_arrive_expect_tx(&sm.full[s], kTileBytes);
+            cctdev::bulk_g2s(sm.ring[s], tiles + (t + kRing) * (int64_t)kTileBytes, kTileBytes, &sm.full[s]);
+        }
     }
-    if (!ok_all) {
+    if (__syncthreads_or(!ok_all)) {
         if (tid == 0) {
             set_timeout(P);
-            for (int s = 0; s < kRing; ++s) (void)cctdev::mbar_wait_bounded(&sm.full[s], 0, 1024);
+            // let the last copy into every slot land before shared memory is given up (earlier
+            // copies into a slot were consumed before its refill)
+            for (int s = 0; s < kRing; ++s)
+                if (sm.last_issued[s] != kNone)
+                    (void)cctdev::mbar_wait_bounded(&sm.full[s], (sm.last_issued[s] / kRing) & 1u, kTmaPolls);
         }
         __syncthreads();
         return false;
