@@ -192,21 +192,14 @@ __device__ void begin_step(const AdjParams &A, int64_t pi, int step) {
     set_weight(A, pi, step, 3, ad + AD_LK);
 }
 
-// Phase C' of stage `stage` (3..0): mu = J_f^T lk, LY += mu, next lk and weight.
-__device__ void end_stage(const AdjParams &A, int64_t pi, int step, int stage) {
+// Phase C' of stage `stage` (3..0): mu = J_f^T lk, LY += mu, next lk and weight; g = the
+// CCT part of grad_p (a . B) (sum of the chunk partials).
+__device__ void end_stage(const AdjParams &A, int64_t pi, int step, int stage, const double g[3]) {
     const TrackParams &P = A.T;
     const double *S = P.state + pi * kStateD;
     if ((double)step >= S[ST_NSTEPS]) return;
     const int d = (int)(pi / P.n_p);
-    const int64_t j = pi % P.n_p, b = j / P.G, slot = j % P.G;
-    const int64_t cd = P.chunks[d], u0 = P.unit_off[d] + b * cd;
-    double mu[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
-    for (int64_t c = 0; c < cd; ++c) {
-        const double *p = P.partial + ((u0 + c) * P.G + slot) * 3;
-        mu[0] += p[0];
-        mu[1] += p[1];
-        mu[2] += p[2];
-    }
+    double mu[6] = {g[0], g[1], g[2], 0.0, 0.0, 0.0};
     const double *rec = rec_at(P, step, stage, pi);
     double *ad = A.adj + pi * kAdjD;
     for (int64_t q = P.qs_off[d]; q < P.qs_off[d + 1]; ++q) qs_grad_add(P.qs + kQsRecord * q, rec, ad + AD_A, mu);
@@ -227,31 +220,41 @@ __device__ void end_stage(const AdjParams &A, int64_t pi, int step, int stage) {
     }
 }
 
-__global__ void __launch_bounds__(kTrackBlock) adjoint_kernel(AdjParams A) {
+__global__ void __launch_bounds__(kTrackBlock, kTrackMinBlocks) adjoint_kernel(AdjParams A) {
     __shared__ __align__(128) TrackSmem sm;
     const TrackParams &P = A.T;
     const int64_t total = (int64_t)P.n_designs * P.n_p;
     const int64_t tstride = (int64_t)gridDim.x * blockDim.x;
     const int64_t n_units = P.unit_off[P.n_designs];
     const int64_t first = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t gwarp = first >> 5, nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     if (A.step_end <= A.step_begin) return;
     if (threadIdx.x == 0) ring_init(sm);
     for (int64_t pi = first; pi < total; pi += tstride) begin_step(A, pi, A.step_end - 1);
+    clear_unit_counters(P);
     if (!grid_barrier(P, sm)) return;
     uint32_t kt = 0;   // tiles consumed through the TMA ring by this CTA (FP32c)
+    int phase = 0;
     for (int step = A.step_end - 1; step >= A.step_begin; --step) {
-        for (int stage = 3; stage >= 0; --stage) {
+        for (int stage = 3; stage >= 0; --stage, ++phase) {
             const PointSrc src{rec_at(P, step, stage, 0), kRec, A.adj + AD_A, kAdjD};
-            bool ok = true;
-            for (int64_t u = blockIdx.x; u < n_units && ok; u += gridDim.x) {
-                if (P.precision == 0) unit_grad_f64(A, u, step, stage, sm);
-                else if (P.ppt == 2) ok = unit_sum_f32c<2, true>(P, src, u, sm, kt);
-                else ok = unit_sum_f32c<1, true>(P, src, u, sm, kt);
+            if (P.precision == 0) {
+                for (int64_t u = next_unit(P, sm, phase); u < n_units; u = next_unit(P, sm, phase))
+                    unit_grad_f64(A, u, step, stage, sm);
+            } else if (P.ppt == 2) {
+                units_f32c<2, true>(P, src, sm, kt, phase, n_units);
+            } else {
+                units_f32c<1, true>(P, src, sm, kt, phase, n_units);
             }
-            if (!grid_barrier(P, sm)) return;
-            for (int64_t pi = first; pi < total; pi += tstride) {
-                end_stage(A, pi, step, stage);
-                if (stage == 0 && step > A.step_begin) begin_step(A, pi, step - 1);
+            if (!grid_barrier(P, sm)) return;   // a TMA timeout is recorded in CW_ERR and ends here
+            reset_next_unit(P, phase);
+            for (int64_t pi = gwarp; pi < total; pi += nwarps) {   // a warp per particle
+                double g[3] = {0.0, 0.0, 0.0};
+                if (particle_active(P, pi, step)) warp_sum_partials(P, pi, g);
+                if ((threadIdx.x & 31) == 0) {
+                    end_stage(A, pi, step, stage, g);
+                    if (stage == 0 && step > A.step_begin) begin_step(A, pi, step - 1);
+                }
             }
             if (!grid_barrier(P, sm)) return;
         }
@@ -508,7 +511,8 @@ static int launch_adjoint(const double *kls, const double *p0s, const int64_t *s
     if (rc != CCT_OK) return rc;
     const int G = group_size(precision, n_p);
     int64_t *unit_off = tables.data(), *chunks = unit_off + n_designs + 1, *chunk_tiles = chunks + n_designs;
-    const int64_t n_units = plan_units(hoff.data(), n_designs, n_p, G, grid, unit_off, chunks, chunk_tiles);
+    const int64_t n_units = plan_units(hoff.data(), n_designs, n_p, G, grid, units_bound(n_designs, n_p, G, grid),
+                                       unit_off, chunks, chunk_tiles);
     const TrackScratchLayout L = track_scratch_layout(n_designs, n_p, n_units, G);
     if (reinterpret_cast<uintptr_t>(scratch) % 256) return set_error(CCT_ERR_ARG, "adjoint scratch must be 256-byte aligned");
     if (scratch_bytes < L.total) return set_error(CCT_ERR_ARG, "adjoint scratch too small (%lld bytes)", (long long)scratch_bytes);

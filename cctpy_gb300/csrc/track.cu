@@ -23,11 +23,13 @@
 #include <mutex>
 #include <vector>
 
+#include <algorithm>
+
 #include "track_common.cuh"
 
 namespace cctgpu {
 
-__global__ void __launch_bounds__(kTrackBlock) track_kernel(TrackParams P) {
+__global__ void __launch_bounds__(kTrackBlock, kTrackMinBlocks) track_kernel(TrackParams P) {
     __shared__ __align__(128) TrackSmem sm;
     const int64_t total = (int64_t)P.n_designs * P.n_p;
     const int64_t tstride = (int64_t)gridDim.x * blockDim.x;
@@ -51,22 +53,33 @@ __global__ void __launch_bounds__(kTrackBlock) track_kernel(TrackParams P) {
         if (!ok) atomicExch(P.ctrl + CW_NONFINITE, 1u);
         else atomicMax(P.ctrl + CW_MAXSTEPS, (unsigned)steps);
     }
+    clear_unit_counters(P);
     if (!grid_barrier(P, sm)) return;
     const int max_steps = P.init_from_records ? (int)*(volatile unsigned *)(P.ctrl + CW_MAXSTEPS) : P.step_end;
     const int step_end = min(max_steps, P.step_end);
     const int64_t n_units = P.unit_off[P.n_designs];
+    const int64_t gwarp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
 
+    int phase = 0;
     for (int step = P.step_begin; step < step_end; ++step) {
-        for (int stage = 0; stage < 4; ++stage) {
-            bool ok = true;
-            for (int64_t u = blockIdx.x; u < n_units && ok; u += gridDim.x) {
-                if (P.precision == 0) unit_field_f64(P, u, sm);
-                else if (P.ppt == 2) ok = unit_field_f32c<2>(P, u, sm, kt);
-                else ok = unit_field_f32c<1>(P, u, sm, kt);
+        for (int stage = 0; stage < 4; ++stage, ++phase) {
+            if (P.precision == 0) {
+                for (int64_t u = next_unit(P, sm, phase); u < n_units; u = next_unit(P, sm, phase))
+                    unit_field_f64(P, u, sm);
+            } else if (P.ppt == 2) {
+                units_f32c<2, false>(P, stage_points(P), sm, kt, phase, n_units);
+            } else {
+                units_f32c<1, false>(P, stage_points(P), sm, kt, phase, n_units);
             }
-            if (!grid_barrier(P, sm)) return;
-            for (int64_t pi = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; pi < total; pi += tstride)
-                particle_update(P, pi, step, stage);
+            if (!grid_barrier(P, sm)) return;   // a TMA timeout is recorded in CW_ERR and ends here
+            reset_next_unit(P, phase);
+            for (int64_t pi = gwarp; pi < total; pi += nwarps) {   // a warp per particle
+                if (!particle_active(P, pi, step)) continue;
+                double B[3];
+                warp_sum_partials(P, pi, B);
+                if ((threadIdx.x & 31) == 0) particle_update(P, pi, step, stage, B);
+            }
             if (!grid_barrier(P, sm)) return;
         }
     }
@@ -103,7 +116,7 @@ TrackScratchLayout track_scratch_layout(int n_designs, int64_t n_particles, int6
 // the batch fills, so that every warp reads every staged tile.
 int group_size(int precision, int64_t n_p) {
     if (precision == 0) return 32;
-    int G = 512;
+    int G = kMaxGroup;
     while (G > 32 && n_p < G) G /= 2;
     return G;
 }
@@ -120,27 +133,48 @@ int track_grid(int *grid_out) {
     return CCT_OK;
 }
 
-static int64_t chunks_wanted(int grid, int n_designs, int64_t blocks) {
-    const int64_t target = (int64_t)kUnitsPerCta * grid;
-    int64_t want = (target + (int64_t)n_designs * blocks - 1) / ((int64_t)n_designs * blocks);
-    return want < 1 ? 1 : (want > kMaxChunks ? kMaxChunks : want);
-}
+static int64_t tiles_of(const int64_t *hoff, int d) { return (hoff[d + 1] - hoff[d] + kTile - 1) / kTile; }
 
-// Fills unit_off[n+1], chunks[n], chunk_tiles[n] (caller storage); returns the unit count.
-int64_t plan_units(const int64_t *hoff, int n_designs, int64_t n_p, int G, int grid, int64_t *unit_off,
-                          int64_t *chunks, int64_t *chunk_tiles) {
+// Units are (design, particle block of G, chunk of ct tiles).  Every chunk of every design
+// spans the same ct tiles (the last one of a design fewer), with ct chosen for about
+// kUnitsPerCta units per CTA and at most max_units units.  Fills unit_off[n+1], chunks[n],
+// chunk_tiles[n] (caller storage); returns the unit count, or -1 if one chunk per (design,
+// block) is already more than max_units.
+int64_t plan_units(const int64_t *hoff, int n_designs, int64_t n_p, int G, int grid, int64_t max_units,
+                   int64_t *unit_off, int64_t *chunks, int64_t *chunk_tiles) {
     const int64_t blocks = (n_p + G - 1) / G;
-    const int64_t want = chunks_wanted(grid, n_designs, blocks);
+    int64_t work = 0, max_nt = 1;
+    for (int d = 0; d < n_designs; ++d) {
+        const int64_t nt = std::max<int64_t>(tiles_of(hoff, d), 1);
+        work += blocks * nt;
+        max_nt = std::max(max_nt, nt);
+    }
+    const int64_t target = std::max<int64_t>(1, std::min<int64_t>((int64_t)kUnitsPerCta * grid, max_units));
+    int64_t ct = std::max<int64_t>({(work + target - 1) / target, (max_nt + kMaxChunks - 1) / kMaxChunks, 1});
+    for (;;) {
+        int64_t units = 0;
+        for (int d = 0; d < n_designs; ++d) {
+            const int64_t nt = tiles_of(hoff, d);
+            units += blocks * (nt > 0 ? (nt + ct - 1) / ct : 1);
+        }
+        if (units <= max_units) break;
+        if (ct >= max_nt) return -1;
+        ct = std::min(max_nt, ct + std::max<int64_t>(1, ct / 8));
+    }
     unit_off[0] = 0;
     for (int d = 0; d < n_designs; ++d) {
-        const int64_t nt = (hoff[d + 1] - hoff[d] + kTile - 1) / kTile;
-        const int64_t ct = nt > 0 ? (nt + want - 1) / want : 1;
+        const int64_t nt = tiles_of(hoff, d);
         const int64_t cd = nt > 0 ? (nt + ct - 1) / ct : 1;
         chunks[d] = cd;
-        chunk_tiles[d] = ct;
+        chunk_tiles[d] = nt > 0 ? ct : 1;
         unit_off[d + 1] = unit_off[d] + blocks * cd;
     }
     return unit_off[n_designs];
+}
+
+// Units the planner may use: kUnitsPerCta per CTA plus one remainder chunk per (design, block).
+int64_t units_bound(int n_designs, int64_t n_p, int G, int grid) {
+    return (int64_t)kUnitsPerCta * grid + (int64_t)n_designs * ((n_p + G - 1) / G);
 }
 
 int64_t track_scratch_bound(int n_designs, int64_t n_particles) {
@@ -152,12 +186,16 @@ int64_t track_scratch_bound(int n_designs, int64_t n_particles) {
     int64_t best = 0;
     for (int prec = 0; prec < 2; ++prec) {
         const int G = group_size(prec, n_particles);
-        const int64_t blocks = (n_particles + G - 1) / G;
-        const int64_t units = (int64_t)n_designs * blocks * chunks_wanted(grid, n_designs, blocks);
-        const int64_t t = track_scratch_layout(n_designs, n_particles, units, G).total;
+        const int64_t t = track_scratch_layout(n_designs, n_particles, units_bound(n_designs, n_particles, G, grid), G).total;
         if (t > best) best = t;
     }
     return best;
+}
+
+// Largest unit count whose partial sums fit in `bytes` of scratch next to the fixed parts.
+static int64_t units_fitting(int n_designs, int64_t n_p, int G, int64_t bytes) {
+    const int64_t fixed = track_scratch_layout(n_designs, n_p, 0, G).total;
+    return bytes > fixed + 256 ? (bytes - fixed - 256) / (24 * (int64_t)G) : 0;
 }
 
 // Shared by both entry points: validate, plan, write the tables, launch, read the status.
@@ -191,13 +229,17 @@ static int run_track(const double *kls, const double *p0s, const int64_t *seg_of
     if (rc != CCT_OK) return rc;
     const int G = group_size(precision, n_particles);
     int64_t *unit_off = tables, *chunks = unit_off + n_designs + 1, *chunk_tiles = chunks + n_designs;
-    const int64_t n_units = plan_units(hoff, n_designs, n_particles, G, grid, unit_off, chunks, chunk_tiles);
-    const TrackScratchLayout L = track_scratch_layout(n_designs, n_particles, n_units, G);
-    if (scratch_bytes < L.total)
+    const int64_t n_units = plan_units(hoff, n_designs, n_particles, G, grid,
+                                       units_fitting(n_designs, n_particles, G, scratch_bytes), unit_off, chunks,
+                                       chunk_tiles);
+    const int64_t blocks = (n_particles + G - 1) / G;
+    const int64_t least = track_scratch_layout(n_designs, n_particles, (int64_t)n_designs * blocks, G).total;
+    if (n_units < 0)
         return set_error(CCT_ERR_ARG,
                          "%d designs x %lld particles need %lld bytes of tracking scratch; the %s holds %lld%s",
-                         n_designs, (long long)n_particles, (long long)L.total, scratch_name, (long long)scratch_bytes,
+                         n_designs, (long long)n_particles, (long long)least, scratch_name, (long long)scratch_bytes,
                          hint);
+    const TrackScratchLayout L = track_scratch_layout(n_designs, n_particles, n_units, G);
     if (reinterpret_cast<uintptr_t>(sc) % 256) return set_error(CCT_ERR_ARG, "tracking scratch must be 256-byte aligned");
     // the scratch keeps a previous call's contents: clear the control words, rewrite the tables
     CCT_TRY_CUDA(cudaMemsetAsync(sc, 0, 256, st));

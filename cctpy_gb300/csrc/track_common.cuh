@@ -9,17 +9,20 @@
 
 namespace cctgpu {
 
-constexpr int kTrackBlock = 256;
+constexpr int kTrackBlock = 64;      // 2 warps; 8 CTAs per SM, which take units dynamically
+constexpr int kTrackMinBlocks = 8;
 constexpr int kTrackWarps = kTrackBlock / 32;
+constexpr int kMaxGroup = 64 * kTrackWarps;   // particles per unit: 2 per lane in every warp
 constexpr int kStateD = 24;          // doubles of RK4 state per particle
 constexpr int kMaxChunks = 4096;     // chunks per (design, block)
-constexpr int kUnitsPerCta = 4;      // target units per CTA and stage (load balance)
+constexpr int kUnitsPerCta = 8;      // target units per CTA and stage (dynamic load balance)
 constexpr int kRing = 4;             // TMA ring depth (tiles)
-constexpr int kRedDoubles = 512 * 3; // per-CTA reduction buffer: S slices x G particles x 3
+constexpr int kTrackUnroll = 2;      // unroll of the 4-segment loop over whole tiles
+constexpr int kRedDoubles = kMaxGroup * 3;   // per-CTA reduction buffer: S slices x G particles x 3
 constexpr uint32_t kTmaPolls = 1u << 22;
 
 // control words
-enum { CW_COUNT = 0, CW_GEN = 1, CW_ERR = 2, CW_NONFINITE = 3, CW_MAXSTEPS = 4 };
+enum { CW_COUNT = 0, CW_GEN = 1, CW_ERR = 2, CW_NONFINITE = 3, CW_MAXSTEPS = 4, CW_NEXT0 = 5, CW_NEXT1 = 6 };
 
 // state layout per particle
 enum { ST_Y0 = 0, ST_YS = 6, ST_KSUM = 12, ST_DT = 18, ST_KQ = 19, ST_NSTEPS = 20 };
@@ -62,6 +65,7 @@ struct TrackSmem {
     uint32_t last_issued[kRing];   // ring tile index last copied into each slot (kNone: none)
     int released[kRing];           // warps done with the slot's current tile
     double red[kRedDoubles];
+    int64_t unit;                  // unit handed to this CTA (dynamic schedule)
     int verdict;
 };
 constexpr uint32_t kNone = 0xffffffffu;
@@ -117,6 +121,28 @@ static __device__ bool grid_barrier(const TrackParams &P, TrackSmem &sm) {
     }
     __syncthreads();
     return sm.verdict != 0;
+}
+
+// Dynamic unit schedule.  Phase k of a launch hands out units from counter CW_NEXT0 + (k & 1);
+// the other counter is cleared during the phase's particle step (reset_next_unit, after the
+// grid barrier that ends the unit phase), so it is zero again when phase k + 1 starts.
+// Every unit writes its partial sums to its own slots, so which CTA takes which unit does
+// not change any result.
+static __device__ __forceinline__ int64_t next_unit(const TrackParams &P, TrackSmem &sm, int phase) {
+    __syncthreads();   // the previous value has been read by every thread
+    if (threadIdx.x == 0) sm.unit = (int64_t)atomicAdd(P.ctrl + CW_NEXT0 + (phase & 1), 1u);
+    __syncthreads();
+    return sm.unit;
+}
+static __device__ __forceinline__ void reset_next_unit(const TrackParams &P, int phase) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicExch(P.ctrl + CW_NEXT0 + ((phase + 1) & 1), 0u);
+}
+// At kernel start, before the first grid barrier.
+static __device__ __forceinline__ void clear_unit_counters(const TrackParams &P) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        atomicExch(P.ctrl + CW_NEXT0, 0u);
+        atomicExch(P.ctrl + CW_NEXT1, 0u);
+    }
 }
 
 // cross product with the reference's component formula (point.py:402-410), unfused
@@ -211,13 +237,32 @@ __device__ __forceinline__ PointSrc stage_points(const TrackParams &P) {
     return PointSrc{P.state + ST_YS, kStateD, nullptr, 0};
 }
 
-// Phase A, FP32c: the chunk's tiles stream through the shared-memory ring (TMA).
-// GRAD = false: field sums B at the points; GRAD = true: gradient sums grad_p (a . B) with
-// the per-point weights of `src`.  `kt` counts the tiles this CTA has consumed so far (ring
-// slot and phase parity).  Returns false if a TMA wait gave up (CCT_ERR_TIMEOUT recorded).
+// Issue the first ring tiles of unit u (thread 0 only; the ring is idle: every tile of the
+// previous unit has been consumed and no refill past a unit's end is ever issued).
+static __device__ __forceinline__ void unit_prefetch(const TrackParams &P, int64_t u, TrackSmem &sm, uint32_t kt) {
+    if (threadIdx.x != 0) return;
+    const UnitRef U = locate_unit(P, u);
+    const unsigned char *tiles = P.tiles + (P.tile_off[U.d] + U.t_beg) * (int64_t)kTileBytes;
+    const int64_t nt = U.t_end - U.t_beg;
+    for (int64_t t = 0; t < kRing && t < nt; ++t) {
+        const int s = (int)((kt + t) % kRing);
+        sm.last_issued[s] = kt + (uint32_t)t;
+        cctdev::fence_proxy_async();
+        cctdev::mbar_arrive_expect_tx(&sm.full[s], kTileBytes);
+        cctdev::bulk_g2s(sm.ring[s], tiles + t * (int64_t)kTileBytes, kTileBytes, &sm.full[s]);
+    }
+}
+
+// Phase A, FP32c, for unit u whose first tiles unit_prefetch has issued: the unit's tiles
+// stream through the shared-memory ring (TMA).  GRAD = false: field sums B at the points;
+// GRAD = true: gradient sums grad_p (a . B) with the per-point weights of `src`.  `kt` counts
+// the tiles this CTA has consumed (ring slot and phase parity).  Once the tiles are done it
+// claims the CTA's next unit of the phase and issues that unit's first tiles, so that their
+// copies overlap this unit's reduction.  Returns the next unit (>= n_units: none), or -1 if a
+// TMA wait gave up (CCT_ERR_TIMEOUT recorded).
 template <int PPT, bool GRAD>
-static __device__ bool unit_sum_f32c(const TrackParams &P, const PointSrc &src, int64_t u, TrackSmem &sm,
-                                     uint32_t &kt) {
+static __device__ int64_t unit_sum_f32c(const TrackParams &P, const PointSrc &src, int64_t u, TrackSmem &sm,
+                                        uint32_t &kt, int phase, int64_t n_units) {
     const UnitRef U = locate_unit(P, u);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int G = P.G;
@@ -245,15 +290,6 @@ static __device__ bool unit_sum_f32c(const TrackParams &P, const PointSrc &src, 
 
     const unsigned char *tiles = P.tiles + (P.tile_off[U.d] + U.t_beg) * (int64_t)kTileBytes;
     const int64_t nt = U.t_end - U.t_beg;
-    if (tid == 0) {   // the ring is idle here: the previous unit ended at a CTA barrier
-        for (int64_t t = 0; t < kRing && t < nt; ++t) {
-            const int s = (int)((kt + t) % kRing);
-            sm.last_issued[s] = kt + (uint32_t)t;
-            cctdev::fence_proxy_async();
-            cctdev::mbar_arrive_expect_tx(&sm.full[s], kTileBytes);
-            cctdev::bulk_g2s(sm.ring[s], tiles + t * (int64_t)kTileBytes, kTileBytes, &sm.full[s]);
-        }
-    }
     // Warps run through the ring independently: a warp waits only for its next tile to
     // land; the last warp done with a slot refills it with the tile kRing further on.
     bool ok_all = true;
@@ -266,6 +302,7 @@ static __device__ bool unit_sum_f32c(const TrackParams &P, const PointSrc &src, 
             break;
         }
         if (GRAD) tile_grad_f32c<PPT>(sm.ring[s], ph, pl, a, acc, g0, g1);
+        else if (S == 1) tile_f32c<PPT, kTrackUnroll>(sm.ring[s], ph, pl, acc);   // whole tiles: fixed trip counts
         else tile_f32c<PPT>(sm.ring[s], ph, pl, acc, g0, g1);
         if (cctdev::ring_release_last(&sm.released[s], kTrackWarps) && t + kRing < nt) {
             sm.last_issued[s] = k + kRing;
@@ -284,9 +321,11 @@ static __device__ bool unit_sum_f32c(const TrackParams &P, const PointSrc &src, 
                     (void)cctdev::mbar_wait_bounded(&sm.full[s], (sm.last_issued[s] / kRing) & 1u, kTmaPolls);
         }
         __syncthreads();
-        return false;
+        return -1;
     }
     kt += (uint32_t)nt;
+    const int64_t next = next_unit(P, sm, phase);   // all warps are past their last tile
+    if (next < n_units) unit_prefetch(P, next, sm, kt);
 
     // reduce the S slices of every particle in fixed order
 #pragma unroll
@@ -311,30 +350,63 @@ static __device__ bool unit_sum_f32c(const TrackParams &P, const PointSrc &src, 
         out[2] = sz;
     }
     __syncthreads();
+    return next;
+}
+
+// All FP32c units of one phase handed to this CTA.  Returns false if a TMA wait gave up.
+template <int PPT, bool GRAD>
+static __device__ bool units_f32c(const TrackParams &P, const PointSrc &src, TrackSmem &sm, uint32_t &kt, int phase,
+                                  int64_t n_units) {
+    int64_t u = next_unit(P, sm, phase);
+    if (u < n_units) unit_prefetch(P, u, sm, kt);
+    while (u < n_units) {
+        u = unit_sum_f32c<PPT, GRAD>(P, src, u, sm, kt, phase, n_units);
+        if (u < 0) return false;
+    }
     return true;
 }
 
-template <int PPT>
-static __device__ __forceinline__ bool unit_field_f32c(const TrackParams &P, int64_t u, TrackSmem &sm, uint32_t &kt) {
-    return unit_sum_f32c<PPT, false>(P, stage_points(P), u, sm, kt);
-}
-
-// Phase C for one particle at RK4 stage `stage` (0..3) of step `step`.
-static __device__ void particle_update(const TrackParams &P, int64_t pi, int step, int stage) {
-    double *S = P.state + pi * kStateD;
-    if ((double)step >= S[ST_NSTEPS]) return;
+// Sum of the chunk partials of particle pi by the calling warp (all 32 lanes, converged):
+// lane l adds chunks l, l + 32, ... in turn, then a fixed shuffle tree; lane 0 gets the
+// total.  A fixed order (deterministic), and the chunk loads of one particle are spread
+// over the warp instead of one thread walking them in sequence.
+static __device__ __forceinline__ void warp_sum_partials(const TrackParams &P, int64_t pi, double out[3]) {
+    const int lane = threadIdx.x & 31;
     const int d = (int)(pi / P.n_p);
     const int64_t j = pi % P.n_p;
     const int64_t b = j / P.G, slot = j % P.G;
     const int64_t cd = P.chunks[d];
     const int64_t u0 = P.unit_off[d] + b * cd;
-    double B[3] = {0.0, 0.0, 0.0};
-    for (int64_t c = 0; c < cd; ++c) {
+    double x = 0.0, y = 0.0, z = 0.0;
+    for (int64_t c = lane; c < cd; c += 32) {
         const double *p = P.partial + ((u0 + c) * P.G + slot) * 3;
-        B[0] += p[0];
-        B[1] += p[1];
-        B[2] += p[2];
+        x += p[0];
+        y += p[1];
+        z += p[2];
     }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        x += __shfl_down_sync(0xffffffffu, x, o);
+        y += __shfl_down_sync(0xffffffffu, y, o);
+        z += __shfl_down_sync(0xffffffffu, z, o);
+    }
+    out[0] = x;
+    out[1] = y;
+    out[2] = z;
+}
+
+// True while particle pi still has RK4 steps at `step`.
+__device__ __forceinline__ bool particle_active(const TrackParams &P, int64_t pi, int step) {
+    return (double)step < P.state[pi * kStateD + ST_NSTEPS];
+}
+
+// Phase C for one particle at RK4 stage `stage` (0..3) of step `step`, given the CCT field
+// B (sum of the chunk partials; QS are added here).
+static __device__ void particle_update(const TrackParams &P, int64_t pi, int step, int stage, const double Bc[3]) {
+    double *S = P.state + pi * kStateD;
+    if ((double)step >= S[ST_NSTEPS]) return;
+    const int d = (int)(pi / P.n_p);
+    double B[3] = {Bc[0], Bc[1], Bc[2]};
     const double *Ys = S + ST_YS;
     for (int64_t q = P.qs_off[d]; q < P.qs_off[d + 1]; ++q)
         qs_field_add(P.qs + kQsRecord * q, Ys[0], Ys[1], Ys[2], B[0], B[1], B[2]);
@@ -390,8 +462,9 @@ extern int g_test_phantom_blocks;
 extern long long g_wait_ms;
 int group_size(int precision, int64_t n_p);
 int track_grid(int *grid_out);
-int64_t plan_units(const int64_t *hoff, int n_designs, int64_t n_p, int G, int grid, int64_t *unit_off,
+int64_t plan_units(const int64_t *hoff, int n_designs, int64_t n_p, int G, int grid, int64_t max_units, int64_t *unit_off,
                    int64_t *chunks, int64_t *chunk_tiles);
+int64_t units_bound(int n_designs, int64_t n_p, int G, int grid);
 cudaError_t launch_track_kernel(TrackParams &P, int grid, cudaStream_t st);
 
 }  // namespace cctgpu

@@ -104,9 +104,12 @@ int cct_field_host(const double *h_kls, const double *h_p0s, int64_t n_seg,
  * steps = ceil(t_end/dt), dt := t_end/steps, Y' = [v, (e/m) v x B(p)],
  * distance += `distance`.
  *
- * One cooperative persistent launch; CTAs meet at bounded grid barriers
- * between RK4 stages.  Needs caller-provided device scratch of
- * cct_track_scratch_bytes() bytes (256-byte aligned).  Returns
+ * One cooperative persistent launch; CTAs take (design, particle block,
+ * segment chunk) units from a per-stage counter and meet at bounded grid
+ * barriers between RK4 stages.  Needs caller-provided device scratch of
+ * cct_track_scratch_bytes() bytes (256-byte aligned); a smaller buffer is
+ * accepted down to the particle state plus one chunk per (design, particle
+ * block), the work then being cut into fewer, larger units.  Returns
  * CCT_ERR_TIMEOUT if a barrier wait gives up and CCT_ERR_NONFINITE if a
  * particle state became non-finite (those particles are still written).
  * Synchronous (reads the device status word before returning).
