@@ -35,6 +35,7 @@ SIGNATURES = {
     "cct_layer_segments": (_i64, [_p, _i32]),
     "cct_segments_build": (ctypes.c_int, [_p, _i32, _p, _p, _i64, _p]),
     "cct_segments_param_grad": (ctypes.c_int, [_p, _i32, _p, _i64, _p, _p]),
+    "cct_beam_readout": (ctypes.c_int, [_p, _i32, _i64, _p, _p, _i32, _i32, _p, _p, _p]),
     "cct_probe_fma_peak": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_double)]),
     "cct_test_set_barrier_fault": (ctypes.c_int, [ctypes.c_int, ctypes.c_int]),
 }

@@ -13,7 +13,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 LIBDIR = os.path.join(HERE, "lib")
 LIB = os.path.join(LIBDIR, "libcctgpu.so")
-SOURCES = ["api.cu", "field.cu", "track.cu", "adjoint.cu", "segments.cu", "diag.cu"]
+SOURCES = ["api.cu", "field.cu", "track.cu", "adjoint.cu", "segments.cu", "readout.cu", "diag.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2"]
 

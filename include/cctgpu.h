@@ -219,6 +219,29 @@ int cct_segments_param_grad(const double *d_layers, int32_t n_layers,
                             const double *d_seg_grad, int64_t n_seg,
                             double *d_param_grad, void *stream);
 
+/* ---------------------------------------------------------------------------
+ * Optimiser read-out.  Replaces the host loop of the reference's optimiser run
+ * script over every design's tracked protons (final_code/work/optim/
+ * A05run.py:247-330): PhaseSpaceParticle.create_from_running_particles
+ * (particles.py:1078-1138) and the BaseUtils.Statistic objectives
+ * (base_utils.py:603-683).  d_particles[n_designs*n_particles*10] are tracked
+ * records (as cct_track leaves them); h_ideal[10] is the ideal particle at the
+ * exit and h_frame[9] its natural frame (XI, YI, ZI).  Writes the phase space
+ * (x, x', y, y', z, delta) of every particle to d_phase_space[...*6]
+ * (required) and, if d_objectives is not NULL, CCT_BEAM_OBJECTIVES values per
+ * design: max|x|, max|x'|, max|y|, max|y'| (mm, mrad), |mean| of the same four,
+ * |max|x| - max|y||, and the spread (max - min) of the half widths in x and in
+ * y of consecutive groups of `group` particles.  speed_from_velocity != 0
+ * first sets each speed to |v| (A05run.py:265-267).  Values are bit-identical
+ * to the reference's (means: CPython 3.12+'s compensated float sum, in list
+ * order).  Asynchronous on `stream`. */
+#define CCT_BEAM_OBJECTIVES 11
+int cct_beam_readout(const double *d_particles, int32_t n_designs,
+                     int64_t n_particles, const double *h_ideal,
+                     const double *h_frame, int32_t group,
+                     int32_t speed_from_velocity, double *d_phase_space,
+                     double *d_objectives, void *stream);
+
 /* Measures the device's fused multiply-add pipe peak (flop/s, 2 per FMA) with
  * independent FMA chains on every SM: kind 0 = scalar FP32, 1 = FP64, 2 = packed
  * FP32x2.  These are the roofline denominators of the field kernels.

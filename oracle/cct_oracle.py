@@ -27,6 +27,7 @@ V3 = Tuple[float, float, float]
 
 # constants: final_code/packages/constants.py:12-19, particles.py:35-47
 MM = 0.001
+MRAD = 1.0 * MM * 1.0          # constants.py:14-15 (RAD = 1)
 LIGHT_SPEED = 299792458.0
 PROTON_STATIC_MASS_KG = 1.672621898e-27
 PROTON_STATIC_ENERGY_MEV = 938.2720813
@@ -577,6 +578,51 @@ def to_phase_space(ideal: numpy.ndarray, frame: Frame, p: numpy.ndarray) -> Tupl
     rmom = sp * float(p[6])
     imom = float(ideal[8]) * float(ideal[6])
     return (x, xp, y, yp, z, (rmom - imom) / imom)
+
+
+# ---------------------------------------------------------------- optimiser read-out
+A05_OBJECTIVES = ("width_max_x", "width_max_xp", "width_max_y", "width_max_yp", "center_x", "center_xp",
+                  "center_y", "center_yp", "diff_xy", "fluct_x", "fluct_y")
+
+
+def beam_objectives(ideal: numpy.ndarray, frame: Frame, finals: numpy.ndarray, group: int = 12,
+                    speed_from_velocity: bool = True) -> Tuple[List[float], List[Tuple[float, ...]]]:
+    """The eleven objectives of one gantry design in the reference's optimiser run script
+    (final_code/work/optim/A05run.py:247-330): speeds reset to |v| (:265-267,
+    P3.length, point.py:327-331), phase space at the exit (to_phase_space), then with the
+    semantics of BaseUtils.Statistic (base_utils.py:603-683; average = sum / len in list
+    order, width = max - min, half_width = width / 2): the largest |x|, |x'|, |y|, |y'| (mm,
+    mrad), |mean| of each, |max|x| - max|y||, and the spread (width) of the half widths in
+    x and in y of consecutive groups of `group` particles."""
+    rows = []
+    for p in finals:
+        q = numpy.array(p, dtype=numpy.float64)
+        if speed_from_velocity:
+            q[8] = math.sqrt(q[3] ** 2 + q[4] ** 2 + q[5] ** 2)
+        rows.append(to_phase_space(ideal, frame, q))
+    xs = [r[0] / MM for r in rows]
+    xps = [r[1] / MRAD for r in rows]
+    ys = [r[2] / MM for r in rows]
+    yps = [r[3] / MRAD for r in rows]
+
+    def average(v):
+        # Statistic.average is sum(data) / len(data) over Python floats (P3 stores floats,
+        # point.py:322-325): on CPython >= 3.12 the builtin sum of floats is Neumaier's
+        # compensated sum, which the GPU read-out restates
+        return sum(float(t) for t in v) / len(v)
+
+    def absolute_max(v):
+        return max(abs(t) for t in v)
+
+    hx, hy = [], []
+    for g in range(0, len(rows), group):
+        gx, gy = xs[g:g + group], ys[g:g + group]
+        hx.append((max(gx) - min(gx)) / 2)
+        hy.append((max(gy) - min(gy)) / 2)
+    wx, wxp, wy, wyp = absolute_max(xs), absolute_max(xps), absolute_max(ys), absolute_max(yps)
+    obj = [wx, wxp, wy, wyp, abs(average(xs)), abs(average(xps)), abs(average(ys)), abs(average(yps)),
+           abs(wx - wy), max(hx) - min(hx), max(hy) - min(hy)]
+    return obj, rows
 
 
 # ---------------------------------------------------------------- RK4 push (base_utils.py, particles.py)
