@@ -191,7 +191,56 @@ def measure_tracking(args, dev, rank):
                      "gpairs_per_s": 512 * (s32 // 2) * 4 * dsp.n_segments / tp / 1e9}}
     if not args.no_adjoint:
         out["design_gradients"] = measure_design_grads(args, rank)
+    if not args.no_generation:
+        out["optimiser_generation"] = measure_generation(args, rank)
     return out
+
+
+def measure_generation(args, rank):
+    """One optimiser generation (the caller loop of the reference's NSGA run script): 64
+    second-section designs, the script's beam (96 protons on the x-x' and y-y' ellipse edges
+    at 4 momentum spreads), tracked through the whole section at the script's 50 mm step,
+    then phase space and the eleven objectives per design.  Timed apart: host beamline build
+    (layer records), device segment generation, FP32c packing, tracking, read-out."""
+    import torch
+    from cctpy_gb300 import HUST_SC_GANTRY, ParticleFactory, engine, workloads as W
+    from cctpy_gb300.optim import a05_phase_space, beam_readout
+
+    kws = W.design_population(64, seed=3 + rank)
+    t0 = time.perf_counter()
+    bls = [HUST_SC_GANTRY(**kw).create_second_bending_part_beamline() for kw in kws]
+    t_host = time.perf_counter() - t0
+    L = bls[0].get_length()
+    ip = ParticleFactory.create_proton_along(bls[0], 0.0, 215.0)
+    beam = ParticleFactory.create_from_phase_space_particles(ip, ip.get_natural_coordinate_system(), a05_phase_space())
+    ip_end = ParticleFactory.create_proton_along(bls[0], L, 215.0)
+    p0 = torch.as_tensor(np.array([b.to_numpy_array_data() for b in beam]), device="cuda")
+    engine.design_set_of(bls[:1], segments="device")          # warm-up
+    torch.cuda.synchronize()
+    t = {}
+    t0 = time.perf_counter()
+    ds = engine.design_set_of(bls, segments="device")
+    torch.cuda.synchronize()
+    t["segments"] = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    ds.packed()
+    torch.cuda.synchronize()
+    t["pack"] = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    final = engine.track(ds, p0, L, 0.05, "f32c")
+    torch.cuda.synchronize()
+    t["track"] = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    _, obj = beam_readout(final, ip_end)
+    obj = obj.cpu().numpy()
+    t["readout"] = time.perf_counter() - t0
+    steps = int(np.ceil(L / 0.05))
+    gpu = sum(t.values())
+    return {"workload": f"64 second-section designs ({ds.n_segments} segments), 96 protons each, {L:.3f} m at 50 mm "
+                        f"({steps} RK4 steps), FP32c; objectives per design as the reference's optimiser script",
+            "host_beamline_seconds": t_host, "device_seconds": t, "generation_seconds_device": gpu,
+            "generations_per_s_device": 1.0 / gpu, "track_gpairs_per_s": 96 * steps * 4 * ds.n_segments / t["track"] / 1e9,
+            "objectives_design0": [float(v) for v in obj[0]]}
 
 
 def measure_design_grads(args, rank):
@@ -433,6 +482,7 @@ def main():
     ap.add_argument("--no-population", action="store_true")
     ap.add_argument("--track-steps", type=int, default=20, help="timed FP32c RK4 steps of the tracking slice")
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--no-generation", action="store_true")
     ap.add_argument("--adjoint-steps", type=int, default=32, help="RK4 steps of the design-gradient slice")
     ap.add_argument("--traffic", type=float, default=None,
                     help="DRAM bytes per launch of the timed kernel from an ncu capture")
