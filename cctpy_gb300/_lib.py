@@ -29,6 +29,13 @@ SIGNATURES = {
     "cct_track": (ctypes.c_int, [_p, _p, _p, _p, _p, _p, _i32, _p, _i64, _d, _d, _i32, _p, _i64, _p]),
     "cct_track_static_scratch_bytes": (_i64, []),
     "cct_track_static_scratch": (ctypes.c_int, [_p, _p, _p, _p, _p, _p, _i32, _p, _i64, _d, _d, _i32, _p]),
+    "cct_track_async": (ctypes.c_int, [_p, _p, _p, _p, _p, _p, _i32, _p, _i64, _d, _d, _i32, _p, _i64, _p]),
+    "cct_track_status": (ctypes.c_int, [_p, _p]),
+    "cct_track_set_units_per_cta": (ctypes.c_int, [_i32]),
+    "cct_track_units_per_cta": (_i32, []),
+    "cct_autotune_scratch_bytes": (_i64, [_i32, _i64]),
+    "cct_autotune": (ctypes.c_int, [_p, _p, _p, _p, _p, _p, _i32, _p, _i64, _d, _i32, _i32, _p, _i64,
+                                    ctypes.POINTER(ctypes.c_int32), _p]),
     "cct_adjoint_scratch_bytes": (_i64, [_i32, _i64, _i32, _i32]),
     "cct_track_adjoint": (ctypes.c_int, [_p, _p, _p, _p, _p, _p, _i32, _p, _i64, _d, _d, _i32, _p, _p, _p, _i32, _p,
                                          _i64, _p]),

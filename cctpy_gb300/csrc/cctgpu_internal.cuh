@@ -50,6 +50,11 @@ TrackScratchLayout track_scratch_layout(int n_designs, int64_t n_particles, int6
 // Upper bound of the scratch any precision needs on the current device (or a generous
 // device-independent bound when no device is visible).
 int64_t track_scratch_bound(int n_designs, int64_t n_particles);
+int launch_track_async(const double *kls, const double *p0s, const int64_t *seg_off, const void *packed,
+                       const double *qs, const int64_t *qs_off, int n_designs, double *particles, int64_t n_p,
+                       double distance, double footstep, int precision, void *scratch, int64_t scratch_bytes,
+                       cudaStream_t st);
+int track_status(const void *scratch, cudaStream_t st);
 int launch_track(const double *kls, const double *p0s, const int64_t *seg_off, const void *packed,
                  const double *qs, const int64_t *qs_off, int n_designs, double *particles, int64_t n_particles,
                  double distance, double footstep, int precision, void *scratch, int64_t scratch_bytes,

@@ -33,6 +33,7 @@ __global__ void __launch_bounds__(kTrackBlock, kTrackMinBlocks) track_kernel(Tra
     __shared__ __align__(128) TrackSmem sm;
     const int64_t total = (int64_t)P.n_designs * P.n_p;
     const int64_t tstride = (int64_t)gridDim.x * blockDim.x;
+    if (*(volatile unsigned *)(P.ctrl + CW_ERR) != 0) return;   // the device-side plan rejected the inputs
     if (threadIdx.x == 0) ring_init(sm);
     uint32_t kt = 0;   // tiles consumed through the ring by this CTA
 
@@ -133,48 +134,17 @@ int track_grid(int *grid_out) {
     return CCT_OK;
 }
 
-static int64_t tiles_of(const int64_t *hoff, int d) { return (hoff[d + 1] - hoff[d] + kTile - 1) / kTile; }
+int g_units_per_cta = kUnitsPerCta;
 
-// Units are (design, particle block of G, chunk of ct tiles).  Every chunk of every design
-// spans the same ct tiles (the last one of a design fewer), with ct chosen for about
-// kUnitsPerCta units per CTA and at most max_units units.  Fills unit_off[n+1], chunks[n],
-// chunk_tiles[n] (caller storage); returns the unit count, or -1 if one chunk per (design,
-// block) is already more than max_units.
 int64_t plan_units(const int64_t *hoff, int n_designs, int64_t n_p, int G, int grid, int64_t max_units,
                    int64_t *unit_off, int64_t *chunks, int64_t *chunk_tiles) {
-    const int64_t blocks = (n_p + G - 1) / G;
-    int64_t work = 0, max_nt = 1;
-    for (int d = 0; d < n_designs; ++d) {
-        const int64_t nt = std::max<int64_t>(tiles_of(hoff, d), 1);
-        work += blocks * nt;
-        max_nt = std::max(max_nt, nt);
-    }
-    const int64_t target = std::max<int64_t>(1, std::min<int64_t>((int64_t)kUnitsPerCta * grid, max_units));
-    int64_t ct = std::max<int64_t>({(work + target - 1) / target, (max_nt + kMaxChunks - 1) / kMaxChunks, 1});
-    for (;;) {
-        int64_t units = 0;
-        for (int d = 0; d < n_designs; ++d) {
-            const int64_t nt = tiles_of(hoff, d);
-            units += blocks * (nt > 0 ? (nt + ct - 1) / ct : 1);
-        }
-        if (units <= max_units) break;
-        if (ct >= max_nt) return -1;
-        ct = std::min(max_nt, ct + std::max<int64_t>(1, ct / 8));
-    }
-    unit_off[0] = 0;
-    for (int d = 0; d < n_designs; ++d) {
-        const int64_t nt = tiles_of(hoff, d);
-        const int64_t cd = nt > 0 ? (nt + ct - 1) / ct : 1;
-        chunks[d] = cd;
-        chunk_tiles[d] = nt > 0 ? ct : 1;
-        unit_off[d + 1] = unit_off[d] + blocks * cd;
-    }
-    return unit_off[n_designs];
+    return plan_units_hd(hoff, n_designs, n_p, G, (int64_t)g_units_per_cta * grid, max_units, unit_off, chunks,
+                         chunk_tiles);
 }
 
-// Units the planner may use: kUnitsPerCta per CTA plus one remainder chunk per (design, block).
+// Units the planner may use: g_units_per_cta per CTA plus one remainder chunk per (design, block).
 int64_t units_bound(int n_designs, int64_t n_p, int G, int grid) {
-    return (int64_t)kUnitsPerCta * grid + (int64_t)n_designs * ((n_p + G - 1) / G);
+    return (int64_t)g_units_per_cta * grid + (int64_t)n_designs * ((n_p + G - 1) / G);
 }
 
 int64_t track_scratch_bound(int n_designs, int64_t n_particles) {
@@ -296,6 +266,126 @@ int launch_track(const double *kls, const double *p0s, const int64_t *seg_off, c
                      hoff.data(), tables.data(), st);
 }
 
+// ---------------------------------------------------------------- asynchronous form
+// cct_track_async: nothing is read back to the host, so the call can be captured in a CUDA
+// graph.  A one-thread kernel checks the offsets (and the packed set) and plans the units
+// on the device; the tracking kernel is launched cooperatively through cudaLaunchKernelEx;
+// the status stays in the scratch's control words for cct_track_status.
+__global__ void plan_kernel(TrackParams P, const unsigned char *packed, int64_t target_units, int64_t max_units,
+                            int64_t *tables) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    unsigned *err = P.ctrl + CW_ERR;
+    int64_t tiles_total = 0;
+    for (int d = 0; d < P.n_designs; ++d) {
+        if (P.seg_off[d + 1] < P.seg_off[d]) {
+            atomicExch(err, (unsigned)CCT_ERR_ARG);
+            return;
+        }
+        tiles_total += tiles_of(P.seg_off, d);
+    }
+    if (P.precision == 1) {
+        const int64_t *h = reinterpret_cast<const int64_t *>(packed);
+        if (h[0] != kPackedMagic || h[1] != P.n_designs || h[2] != tiles_total) {
+            atomicExch(err, (unsigned)CCT_ERR_ARG);
+            return;
+        }
+    }
+    int64_t *unit_off = tables, *chunks = unit_off + P.n_designs + 1, *chunk_tiles = chunks + P.n_designs;
+    if (plan_units_hd(P.seg_off, P.n_designs, P.n_p, P.G, target_units, max_units, unit_off, chunks, chunk_tiles) < 0)
+        atomicExch(err, (unsigned)CCT_ERR_ARG);
+}
+
+static int g_async_grid[64];   // cached cooperative grid per device (occupancy queries stay out of captures)
+
+int launch_track_async(const double *kls, const double *p0s, const int64_t *seg_off, const void *packed,
+                       const double *qs, const int64_t *qs_off, int n_designs, double *particles, int64_t n_p,
+                       double distance, double footstep, int precision, void *scratch, int64_t scratch_bytes,
+                       cudaStream_t st) {
+    int dev = 0;
+    CCT_TRY_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) return set_error(CCT_ERR_UNSUPPORTED, "device index %d", dev);
+    if (!g_async_grid[dev]) {
+        int grid = 0;
+        const int rc = track_grid(&grid);
+        if (rc != CCT_OK) return rc;
+        g_async_grid[dev] = grid;
+    }
+    const int grid = g_async_grid[dev];
+    unsigned char *sc = static_cast<unsigned char *>(scratch);
+    if (reinterpret_cast<uintptr_t>(sc) % 256) return set_error(CCT_ERR_ARG, "tracking scratch must be 256-byte aligned");
+    const int G = group_size(precision, n_p);
+    const int64_t max_units = units_fitting(n_designs, n_p, G, scratch_bytes);
+    if (max_units < (int64_t)n_designs * ((n_p + G - 1) / G))
+        return set_error(CCT_ERR_ARG, "%d designs x %lld particles need at least %lld bytes of tracking scratch, %lld given",
+                         n_designs, (long long)n_p,
+                         (long long)track_scratch_layout(n_designs, n_p, (int64_t)n_designs * ((n_p + G - 1) / G), G).total,
+                         (long long)scratch_bytes);
+    const TrackScratchLayout L = track_scratch_layout(n_designs, n_p, max_units, G);
+    TrackParams P;
+    P.kls = kls;
+    P.p0s = p0s;
+    P.seg_off = seg_off;
+    P.tiles = precision == 1 ? static_cast<const unsigned char *>(packed) + kPackedHeaderBytes +
+                                   packed_index_bytes(n_designs)
+                             : nullptr;
+    P.tile_off = precision == 1
+                     ? reinterpret_cast<const int64_t *>(static_cast<const unsigned char *>(packed) + kPackedHeaderBytes)
+                     : nullptr;
+    P.qs = qs;
+    P.qs_off = qs_off;
+    P.n_designs = n_designs;
+    P.G = G;
+    P.ppt = G >= 64 ? 2 : 1;
+    P.n_p = n_p;
+    P.particles = particles;
+    P.distance = distance;
+    P.footstep = footstep;
+    P.state = reinterpret_cast<double *>(sc + L.state_off);
+    P.partial = reinterpret_cast<double *>(sc + L.partial_off);
+    P.ctrl = reinterpret_cast<unsigned *>(sc);
+    P.unit_off = reinterpret_cast<const int64_t *>(sc + 256);
+    P.chunks = P.unit_off + n_designs + 1;
+    P.chunk_tiles = P.chunks + n_designs;
+    P.precision = precision;
+    P.barrier_blocks = (unsigned)(grid + g_test_phantom_blocks);
+    P.wait_ns = (unsigned long long)g_wait_ms * 1000000ull;
+    P.init_from_records = 1;
+    P.write_back = 1;
+    P.step_begin = 0;
+    P.step_end = 0x7fffffff;
+    P.record = nullptr;
+    CCT_TRY_CUDA(cudaMemsetAsync(sc, 0, 256, st));
+    plan_kernel<<<1, 32, 0, st>>>(P, static_cast<const unsigned char *>(packed), (int64_t)g_units_per_cta * grid,
+                                  max_units, reinterpret_cast<int64_t *>(sc + 256));
+    CCT_TRY_CUDA(cudaGetLastError());
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(kTrackBlock);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    CCT_TRY_CUDA(cudaLaunchKernelEx(&cfg, track_kernel, P));
+    return CCT_OK;
+}
+
+int track_status(const void *scratch, cudaStream_t st) {
+    unsigned ctrl[8];
+    CCT_TRY_CUDA(cudaMemcpyAsync(ctrl, scratch, sizeof ctrl, cudaMemcpyDeviceToHost, st));
+    CCT_TRY_CUDA(cudaStreamSynchronize(st));
+    if ((int)ctrl[CW_ERR] == CCT_ERR_TIMEOUT)
+        return set_error(CCT_ERR_TIMEOUT, "a tracking grid barrier or tile copy waited longer than its limit (%lld ms)",
+                         g_wait_ms);
+    if ((int)ctrl[CW_ERR] == CCT_ERR_ARG)
+        return set_error(CCT_ERR_ARG, "the tracking plan rejected its inputs: segment offsets decrease, the packed set "
+                                      "does not match them, or the scratch is too small");
+    if (ctrl[CW_NONFINITE]) return set_error(CCT_ERR_NONFINITE, "a particle state or step count was not finite");
+    return CCT_OK;
+}
+
 }  // namespace cctgpu
 
 extern "C" int cct_test_set_barrier_fault(int phantom_blocks, int wait_ms) {
@@ -304,6 +394,115 @@ extern "C" int cct_test_set_barrier_fault(int phantom_blocks, int wait_ms) {
     cctgpu::g_test_phantom_blocks = phantom_blocks < 0 ? 0 : phantom_blocks;
     cctgpu::g_wait_ms = wait_ms > 0 ? wait_ms : 60000;
     return CCT_OK;
+}
+
+// ---------------------------------------------------------------- asynchronous form, tuning
+extern "C" int cct_track_async(const double *d_kls, const double *d_p0s, const int64_t *d_seg_off,
+                               const void *d_packed, const double *d_qs, const int64_t *d_qs_off, int32_t n_designs,
+                               double *d_particles, int64_t n_particles, double distance, double footstep,
+                               int32_t precision, void *d_scratch, int64_t scratch_bytes, void *stream) {
+    using namespace cctgpu;
+    clear_error();
+    if (n_designs <= 0 || n_particles <= 0) return set_error(CCT_ERR_ARG, "need at least one design and particle");
+    if (!d_seg_off || !d_particles || !d_scratch) return set_error(CCT_ERR_ARG, "null offsets, particles or scratch");
+    if (precision != 0 && precision != 1) return set_error(CCT_ERR_ARG, "precision must be 0 (FP64) or 1 (FP32c)");
+    if (precision == 0 && (!d_kls || !d_p0s)) return set_error(CCT_ERR_ARG, "FP64 tracking needs d_kls and d_p0s");
+    if (precision == 1 && !d_packed) return set_error(CCT_ERR_ARG, "FP32c tracking needs the packed segments");
+    if (!(distance >= 0.0) || !(footstep > 0.0)) return set_error(CCT_ERR_ARG, "distance >= 0 and footstep > 0 needed");
+    return launch_track_async(d_kls, d_p0s, d_seg_off, d_packed, d_qs, d_qs_off, n_designs, d_particles, n_particles,
+                              distance, footstep, precision, d_scratch, scratch_bytes,
+                              static_cast<cudaStream_t>(stream));
+}
+
+extern "C" int cct_track_status(const void *d_scratch, void *stream) {
+    cctgpu::clear_error();
+    if (!d_scratch) return cctgpu::set_error(CCT_ERR_ARG, "null scratch");
+    return cctgpu::track_status(d_scratch, static_cast<cudaStream_t>(stream));
+}
+
+extern "C" int cct_track_set_units_per_cta(int32_t units_per_cta) {
+    cctgpu::clear_error();
+    if (units_per_cta < 0 || units_per_cta > 64)
+        return cctgpu::set_error(CCT_ERR_ARG, "units per CTA %d (1..64, 0 = default)", units_per_cta);
+    cctgpu::g_units_per_cta = units_per_cta == 0 ? cctgpu::kUnitsPerCta : units_per_cta;
+    return CCT_OK;
+}
+
+extern "C" int32_t cct_track_units_per_cta(void) { return cctgpu::g_units_per_cta; }
+
+namespace cctgpu {
+static const int kTuneCandidates[] = {2, 4, 8, 16, 32};
+static int64_t up256(int64_t b) { return (b + 255) / 256 * 256; }
+}
+
+extern "C" int64_t cct_autotune_scratch_bytes(int32_t n_designs, int64_t n_particles) {
+    using namespace cctgpu;
+    clear_error();
+    if (n_designs <= 0 || n_particles <= 0) {
+        set_error(CCT_ERR_ARG, "need at least one design and particle");
+        return -1;
+    }
+    const int saved = g_units_per_cta;
+    g_units_per_cta = kTuneCandidates[sizeof kTuneCandidates / sizeof kTuneCandidates[0] - 1];
+    const int64_t t = track_scratch_bound(n_designs, n_particles);
+    g_units_per_cta = saved;
+    return up256(80 * (int64_t)n_designs * n_particles) + t;
+}
+
+extern "C" int cct_autotune(const double *d_kls, const double *d_p0s, const int64_t *d_seg_off, const void *d_packed,
+                            const double *d_qs, const int64_t *d_qs_off, int32_t n_designs,
+                            const double *d_particles, int64_t n_particles, double footstep, int32_t precision,
+                            int32_t steps, void *d_scratch, int64_t scratch_bytes, int32_t *units_per_cta_out,
+                            void *stream) {
+    using namespace cctgpu;
+    clear_error();
+    if (n_designs <= 0 || n_particles <= 0 || steps < 1 || !(footstep > 0.0))
+        return set_error(CCT_ERR_ARG, "need designs, particles, steps >= 1 and footstep > 0");
+    if (!d_particles || !d_scratch || !units_per_cta_out) return set_error(CCT_ERR_ARG, "null particles, scratch or output");
+    const int64_t copy = up256(80 * (int64_t)n_designs * n_particles);
+    if (scratch_bytes < cct_autotune_scratch_bytes(n_designs, n_particles))
+        return set_error(CCT_ERR_ARG, "autotune needs %lld bytes of scratch, %lld given",
+                         (long long)cct_autotune_scratch_bytes(n_designs, n_particles), (long long)scratch_bytes);
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    unsigned char *sc = static_cast<unsigned char *>(d_scratch);
+    double *work = reinterpret_cast<double *>(sc);
+    const int saved = g_units_per_cta;
+    cudaEvent_t a = nullptr, b = nullptr;
+    CCT_TRY_CUDA(cudaEventCreate(&a));
+    CCT_TRY_CUDA(cudaEventCreate(&b));
+    float best_ms = 3.4e38f;
+    int best = saved, rc = CCT_OK;
+    const int n_cand = (int)(sizeof kTuneCandidates / sizeof kTuneCandidates[0]);
+    for (int i = -1; i < n_cand && rc == CCT_OK; ++i) {        // i = -1: warm-up with the current setting
+        g_units_per_cta = i < 0 ? saved : kTuneCandidates[i];
+        cudaError_t e = cudaMemcpyAsync(work, d_particles, 80 * (size_t)n_designs * n_particles,
+                                        cudaMemcpyDeviceToDevice, st);
+        if (e == cudaSuccess) e = cudaEventRecord(a, st);
+        if (e != cudaSuccess) {
+            rc = check_cuda(e, "autotune copy");
+            break;
+        }
+        rc = launch_track(d_kls, d_p0s, d_seg_off, d_packed, d_qs, d_qs_off, n_designs, work, n_particles,
+                          steps * footstep, footstep, precision, sc + copy, scratch_bytes - copy, st);
+        if (rc != CCT_OK) break;
+        e = cudaEventRecord(b, st);
+        if (e == cudaSuccess) e = cudaEventSynchronize(b);
+        float ms = 0.0f;
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, a, b);
+        if (e != cudaSuccess) {
+            rc = check_cuda(e, "autotune timing");
+            break;
+        }
+        if (i >= 0 && ms < best_ms) {
+            best_ms = ms;
+            best = kTuneCandidates[i];
+        }
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    g_units_per_cta = rc == CCT_OK ? best : saved;
+    if (rc == CCT_OK) *units_per_cta_out = best;
+    return rc;
 }
 
 // ============================================================================

@@ -15,7 +15,7 @@ constexpr int kTrackWarps = kTrackBlock / 32;
 constexpr int kMaxGroup = 64 * kTrackWarps;   // particles per unit: 2 per lane in every warp
 constexpr int kStateD = 24;          // doubles of RK4 state per particle
 constexpr int kMaxChunks = 4096;     // chunks per (design, block)
-constexpr int kUnitsPerCta = 8;      // target units per CTA and stage (dynamic load balance)
+constexpr int kUnitsPerCta = 8;      // default target units per CTA and stage (dynamic load balance)
 constexpr int kRing = 4;             // TMA ring depth (tiles)
 constexpr int kTrackUnroll = 2;      // unroll of the 4-segment loop over whole tiles
 constexpr int kRedDoubles = kMaxGroup * 3;   // per-CTA reduction buffer: S slices x G particles x 3
@@ -457,7 +457,54 @@ static __device__ void particle_update(const TrackParams &P, int64_t pi, int ste
     }
 }
 
+// ---------------------------------------------------------------- unit planner (host and device)
+__host__ __device__ inline int64_t hd_max(int64_t a, int64_t b) { return a > b ? a : b; }
+__host__ __device__ inline int64_t hd_min(int64_t a, int64_t b) { return a < b ? a : b; }
+__host__ __device__ inline int64_t tiles_of(const int64_t *seg_off, int d) {
+    return (seg_off[d + 1] - seg_off[d] + kTile - 1) / kTile;
+}
+
+// Units are (design, particle block of G, chunk of ct tiles).  Every chunk of every design
+// spans the same ct tiles (the last one of a design fewer), with ct chosen for about
+// target_units units and at most max_units.  Fills unit_off[n+1], chunks[n], chunk_tiles[n];
+// returns the unit count, or -1 if one chunk per (design, block) is already more than
+// max_units.  The host plans cct_track's units with it, a one-thread kernel those of
+// cct_track_async.
+__host__ __device__ inline int64_t plan_units_hd(const int64_t *seg_off, int n_designs, int64_t n_p, int G,
+                                                 int64_t target_units, int64_t max_units, int64_t *unit_off,
+                                                 int64_t *chunks, int64_t *chunk_tiles) {
+    const int64_t blocks = (n_p + G - 1) / G;
+    int64_t work = 0, max_nt = 1;
+    for (int d = 0; d < n_designs; ++d) {
+        const int64_t nt = hd_max(tiles_of(seg_off, d), 1);
+        work += blocks * nt;
+        max_nt = hd_max(max_nt, nt);
+    }
+    const int64_t target = hd_max(1, hd_min(target_units, max_units));
+    int64_t ct = hd_max(hd_max((work + target - 1) / target, (max_nt + kMaxChunks - 1) / kMaxChunks), 1);
+    for (;;) {
+        int64_t units = 0;
+        for (int d = 0; d < n_designs; ++d) {
+            const int64_t nt = tiles_of(seg_off, d);
+            units += blocks * (nt > 0 ? (nt + ct - 1) / ct : 1);
+        }
+        if (units <= max_units) break;
+        if (ct >= max_nt) return -1;
+        ct = hd_min(max_nt, ct + hd_max(1, ct / 8));
+    }
+    unit_off[0] = 0;
+    for (int d = 0; d < n_designs; ++d) {
+        const int64_t nt = tiles_of(seg_off, d);
+        const int64_t cd = nt > 0 ? (nt + ct - 1) / ct : 1;
+        chunks[d] = cd;
+        chunk_tiles[d] = nt > 0 ? ct : 1;
+        unit_off[d + 1] = unit_off[d] + blocks * cd;
+    }
+    return unit_off[n_designs];
+}
+
 // ---------------------------------------------------------------- host helpers (track.cu)
+extern int g_units_per_cta;
 extern int g_test_phantom_blocks;
 extern long long g_wait_ms;
 int group_size(int precision, int64_t n_p);

@@ -341,3 +341,74 @@ def track(ds: DesignSet, particles, distance: float, footstep: float, precision:
                        prec, sc.data_ptr(), int(nbytes), _stream())
     _lib.check(rc, "cct_track")
     return p.cpu().numpy() if as_numpy else p
+
+
+def _track_args(ds: DesignSet, precision: str):
+    prec = {"f64": 0, "f32c": 1}.get(precision)
+    if prec is None:
+        raise ValueError(f"precision must be 'f64' or 'f32c', not {precision!r}")
+    packed = ds.packed().data_ptr() if prec == 1 else 0
+    return prec, packed
+
+
+class TrackLaunch:
+    """cct_track_async on device buffers that stay in place, so that the launch can be
+    captured in a CUDA graph (torch.cuda.graph) and replayed: `particles` is a CUDA tensor
+    (n_designs, n, 10) tracked in place; call status() after the launch (or the replay) has
+    been enqueued to synchronise and raise on an error."""
+
+    def __init__(self, ds: DesignSet, particles: torch.Tensor, distance: float, footstep: float,
+                 precision: str = "f32c"):
+        if not (isinstance(particles, torch.Tensor) and particles.is_cuda and particles.dtype == torch.float64
+                and particles.ndim == 3 and particles.shape[0] == ds.n_designs and particles.shape[2] == 10
+                and particles.is_contiguous()):
+            raise ValueError("particles must be a contiguous CUDA float64 tensor (n_designs, n, 10)")
+        self.ds, self.particles = ds, particles
+        self.distance, self.footstep = float(distance), float(footstep)
+        self.prec, self.packed = _track_args(ds, precision)
+        lib = _lib.load()
+        n = lib.cct_track_scratch_bytes(ds.n_designs, particles.shape[1])
+        _lib.check(0 if n >= 0 else _lib.CCT_ERR_ARG, "cct_track_scratch_bytes")
+        self._buf = torch.empty(int(n) + 256, dtype=torch.uint8, device=particles.device)
+        shift = (-self._buf.data_ptr()) % 256
+        self.scratch = self._buf[shift:shift + int(n)]
+
+    def launch(self) -> None:
+        lib = _lib.load()
+        ds = self.ds
+        rc = lib.cct_track_async(_ptr(ds.kls), _ptr(ds.p0s), _ptr(ds.seg_off), self.packed, _ptr(ds.qs),
+                                 _ptr(ds.qs_off), ds.n_designs, self.particles.data_ptr(), self.particles.shape[1],
+                                 self.distance, self.footstep, self.prec, self.scratch.data_ptr(),
+                                 self.scratch.numel(), _stream())
+        _lib.check(rc, "cct_track_async")
+
+    def status(self) -> None:
+        _lib.check(_lib.load().cct_track_status(self.scratch.data_ptr(), _stream()), "cct_track_status")
+
+
+def autotune(ds: DesignSet, particles, footstep: float, precision: str = "f32c", steps: int = 4) -> int:
+    """Time `steps` RK4 steps of this problem for several work splits (units of design x
+    particle block x segment chunk per CTA), keep the fastest for later tracking calls of the
+    process and return it (cct_autotune)."""
+    lib = _lib.load()
+    dev = ds.kls.device
+    p = torch.as_tensor(np.asarray(particles, dtype=np.float64) if not isinstance(particles, torch.Tensor)
+                        else particles, dtype=torch.float64, device=dev)
+    if p.ndim == 2:
+        p = p.unsqueeze(0).expand(ds.n_designs, -1, -1)
+    p = p.contiguous()
+    prec, packed = _track_args(ds, precision)
+    n = lib.cct_autotune_scratch_bytes(ds.n_designs, p.shape[1])
+    _lib.check(0 if n >= 0 else _lib.CCT_ERR_ARG, "cct_autotune_scratch_bytes")
+    sc = scratch(int(n), dev)
+    best = ctypes.c_int32(0)
+    rc = lib.cct_autotune(_ptr(ds.kls), _ptr(ds.p0s), _ptr(ds.seg_off), packed, _ptr(ds.qs), _ptr(ds.qs_off),
+                          ds.n_designs, p.data_ptr(), p.shape[1], float(footstep), prec, int(steps), sc.data_ptr(),
+                          int(n), ctypes.byref(best), _stream())
+    _lib.check(rc, "cct_autotune")
+    return int(best.value)
+
+
+def set_units_per_cta(n: int = 0) -> None:
+    """Set the tracking work split by hand (0 restores the default of 8)."""
+    _lib.check(_lib.load().cct_track_set_units_per_cta(int(n)), "cct_track_set_units_per_cta")

@@ -124,6 +124,44 @@ int cct_track(const double *d_kls, const double *d_p0s, const int64_t *d_seg_off
               double distance, double footstep, int32_t precision,
               void *d_scratch, int64_t scratch_bytes, void *stream);
 
+/* Asynchronous form of cct_track, for pipelines and CUDA-graph capture: the
+ * same arguments and results, but nothing is read back to the host.  A
+ * one-thread kernel checks the segment offsets and the packed set and plans
+ * the units on the device, then the tracking kernel is launched cooperatively
+ * (cudaLaunchKernelEx); both are ordinary stream work, so the call can be
+ * captured into a graph and replayed (the inputs are read at replay time).
+ * The status stays in the scratch: cct_track_status(d_scratch, stream)
+ * synchronises `stream` and returns CCT_OK, CCT_ERR_ARG (inputs rejected by
+ * the plan), CCT_ERR_TIMEOUT or CCT_ERR_NONFINITE.  The first call on a
+ * device queries its occupancy; make it before any capture.  No counterpart in
+ * the reference, whose GPU calls are synchronous. */
+int cct_track_async(const double *d_kls, const double *d_p0s,
+                    const int64_t *d_seg_off, const void *d_packed,
+                    const double *d_qs, const int64_t *d_qs_off,
+                    int32_t n_designs, double *d_particles, int64_t n_particles,
+                    double distance, double footstep, int32_t precision,
+                    void *d_scratch, int64_t scratch_bytes, void *stream);
+int cct_track_status(const void *d_scratch, void *stream);
+
+/* Work split of the tracking kernels: units of (design, particle block,
+ * segment chunk) per CTA and RK4 stage (default 8; 1..64, 0 restores the
+ * default).  Process-wide.  cct_autotune times a few RK4 steps of the caller's
+ * problem (`steps` steps of `footstep`, on a copy of d_particles, which is not
+ * modified) for 2, 4, 8, 16 and 32 units per CTA, keeps the fastest and
+ * returns it; it needs cct_autotune_scratch_bytes() of scratch.  Stands in for
+ * the reference's block_dim_x choice (GPU_ACCELERATOR(block_dim_x=...),
+ * gpu_accelerator.py:54-96), which the caller sets by hand.  Synchronous. */
+int cct_track_set_units_per_cta(int32_t units_per_cta);
+int32_t cct_track_units_per_cta(void);
+int64_t cct_autotune_scratch_bytes(int32_t n_designs, int64_t n_particles);
+int cct_autotune(const double *d_kls, const double *d_p0s,
+                 const int64_t *d_seg_off, const void *d_packed,
+                 const double *d_qs, const int64_t *d_qs_off,
+                 int32_t n_designs, const double *d_particles,
+                 int64_t n_particles, double footstep, int32_t precision,
+                 int32_t steps, void *d_scratch, int64_t scratch_bytes,
+                 int32_t *units_per_cta_out, void *stream);
+
 /* ---------------------------------------------------------------------------
  * Adjoint (gradients): no counterpart in the reference, which has no
  * derivatives; it differentiates cct_track's FP64 forward (the reference's RK4
