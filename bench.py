@@ -34,6 +34,10 @@ if ROOT not in sys.path:
 N_POINTS = 1 << 20
 N_SEG = 46080
 FLOPS_PER_PAIR = 26
+# dram__bytes_read.sum + dram__bytes_write.sum of one field_f32c_kernel launch on the field map
+# (ncu --section MemoryWorkloadAnalysis ...; profiles/field_f32c_field_map.md): the 25 MB of
+# points and 1.7 MB of tiles read; the 25 MB of fields written are still in L2 at the end.
+FIELD_MAP_TRAFFIC_BYTES = 27.3e6
 METRIC = "Biot-Savart Gpairs/s & design-grads/s, 1 GB300: FP32+comp vs FP64 @1e-7 rel"
 WORKLOAD = "field_map: 2^20 points x 46080-segment single CCT dipole"
 
@@ -445,7 +449,11 @@ def run_ours(args):
                     "d2h_bytes_per_step": N_POINTS * 24,
                     "call": "engine.field_at_points(design, pinned host points, 'f32c', out_host=pinned)"},
             "roofline": {"bound": "fp32-pipe", "achieved": achieved, "peak": peak32, "unit": "TFLOP/s",
-                         "frac": achieved / peak32, "traffic": args.traffic,
+                         "frac": achieved / peak32,
+                         "traffic": args.traffic if args.traffic is not None else
+                         (FIELD_MAP_TRAFFIC_BYTES if N_POINTS == 1 << 20 else None),
+                         "traffic_unit": "bytes per launch (dram read + write, ncu capture of this kernel on this "
+                                         "workload: profiles/field_f32c_field_map.md)",
                          "peak_source": "measured in this run: best of scalar FFMA and packed FP32x2 FMA "
                                         "chains (cct_probe_fma_peak)",
                          "peak_scalar_ffma": peak32_scalar, "peak_packed_ffma2": peak32_packed,
@@ -485,7 +493,8 @@ def main():
     ap.add_argument("--no-generation", action="store_true")
     ap.add_argument("--adjoint-steps", type=int, default=32, help="RK4 steps of the design-gradient slice")
     ap.add_argument("--traffic", type=float, default=None,
-                    help="DRAM bytes per launch of the timed kernel from an ncu capture")
+                    help="DRAM bytes per launch of the timed kernel from an ncu capture (default: the committed "
+                         "capture of the field-map launch)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3
