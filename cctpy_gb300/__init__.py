@@ -11,14 +11,16 @@ behind cctpy's own Python API:
 
 Compute runs in libcctgpu.so (C ABI, include/cctgpu.h); there is no CPU path.
 """
-from .geometry import (LIGHT_SPEED, MM, MRAD, ArcLine2, Line2, LocalCoordinateSystem, P2, P3, StraightLine2,
-                       Trajectory)
-from .magnets import CCT, QS, CombinedMagnet, Magnet
+from .geometry import (LIGHT_SPEED, MM, MRAD, ArcLine2, FunctionLine3, Line2, LocalCoordinateSystem, P2, P3,
+                       StraightLine2, Trajectory)
+from .magnets import (AGCCT_CONNECTOR, CCT, QS, CombinedMagnet, LocalUniformMagnet, Magnet, Q, UniformMagnet,
+                      Wire)
 from .beamline import HUST_SC_GANTRY, Beamline
 from .particles import (Ellipse, ParticleFactory, ParticleRunner, PhaseSpaceParticle, Protons, RunningParticle)
 from .accelerator import GPU_ACCELERATOR
 
 __all__ = ["LIGHT_SPEED", "MM", "MRAD", "ArcLine2", "Line2", "LocalCoordinateSystem", "P2", "P3", "StraightLine2",
-           "Trajectory", "CCT", "QS", "CombinedMagnet", "Magnet", "HUST_SC_GANTRY", "Beamline", "Ellipse",
+           "Trajectory", "FunctionLine3", "CCT", "QS", "Q", "LocalUniformMagnet", "UniformMagnet", "Wire",
+           "AGCCT_CONNECTOR", "CombinedMagnet", "Magnet", "HUST_SC_GANTRY", "Beamline", "Ellipse",
            "ParticleFactory", "ParticleRunner", "PhaseSpaceParticle", "Protons", "RunningParticle",
            "GPU_ACCELERATOR"]

@@ -61,6 +61,11 @@ class GPU_ACCELERATOR:
 
     # ------------------------------------------------------------------ helpers
     def _design(self, magnets: list, single_qs: bool = False):
+        for m in magnets:
+            if engine._classify(m) not in ("cct", "qs"):
+                # the reference accelerator takes CCT and QS only (gpu_accelerator.py:1417, :1970)
+                raise ValueError(f"GPU_ACCELERATOR evaluates CCT and QS magnets only, not {m}; use "
+                                 "cctpy_gb300.engine for Q, LocalUniformMagnet, UniformMagnet, Wire and connectors")
         kl, p0, qs = engine.host_design(magnets)
         if single_qs and qs.shape[0] > 1:
             qs = qs[-1:]      # the single-QS kernels of the reference keep the last QS

@@ -15,7 +15,7 @@ import math
 from typing import List, Optional, Tuple
 
 from .geometry import MM, P2, P3, Line2, Trajectory
-from .magnets import CCT, QS, Magnet
+from .magnets import CCT, QS, LocalUniformMagnet, Magnet, Q
 
 
 def _rad(d: float) -> float:
@@ -83,6 +83,26 @@ class Beamline(Line2, Magnet):
         qs = QS.create_qs_along(self.trajectory, old, length, gradient, second_gradient, aperture_radius)
         self.magnets.append(qs)
         self.elements.append((old, qs, length))
+        return self._changed()
+
+    def append_q(self, length: float, gradient: float, aperture_radius: float) -> "Beamline":
+        """A hard-edge quadrupole along the orbit (beamline.py:478-505)."""
+        old = self.trajectory.get_length()
+        self.trajectory.add_strait_line(length=length)
+        q = Q.create_q_along(self.trajectory, old, length, gradient, aperture_radius)
+        self.magnets.append(q)
+        self.elements.append((old, q, length))
+        return self._changed()
+
+    def append_straight_dipole_magnet(self, magnetic_field: float, length: float,
+                                      aperture_radius: float) -> "Beamline":
+        """A straight dipole (LocalUniformMagnet) along the orbit (beamline.py:420-444)."""
+        old = self.trajectory.get_length()
+        self.trajectory.add_strait_line(length=length)
+        lum = LocalUniformMagnet.create_local_uniform_magnet_along(self.trajectory, old, magnetic_field, length,
+                                                                   aperture_radius)
+        self.magnets.append(lum)
+        self.elements.append((old, lum, length))
         return self._changed()
 
     def append_dipole_cct(self, big_r: float, small_r_inner: float, small_r_outer: float, bending_angle: float,

@@ -138,6 +138,7 @@ __device__ void unit_grad_f64(const AdjParams &A, int64_t u, int step, int stage
 // grad_p (a . B_qs) of one QS magnet (magnets.py:637-668: bx = g y + s x y,
 // by = g x + s (x^2 - y^2) / 2 in the local frame, zero outside); added to g.
 __device__ __forceinline__ void qs_grad_add(const double *q, const double *p, const double *a, double *g) {
+    if (q[12] < 0.0) return;   // straight dipole / uniform field: piecewise constant, no gradient
     const double dx = p[0] - q[0], dy = p[1] - q[1], dz = p[2] - q[2];
     const double x = q[3] * dx + q[4] * dy + q[5] * dz;
     const double y = q[6] * dx + q[7] * dy + q[8] * dz;

@@ -165,7 +165,6 @@ int cct_track(const double *d_kls, const double *d_p0s, const int64_t *d_seg_off
         return set_error(CCT_ERR_ARG, "distance (%g) and footstep (%g) must be positive", distance, footstep);
     if (precision != 0 && precision != 1) return set_error(CCT_ERR_ARG, "precision must be 0 or 1");
     if (!d_seg_off || !d_qs_off || !d_particles || !d_scratch) return set_error(CCT_ERR_ARG, "null pointer");
-    if (precision == 0 && (!d_kls || !d_p0s)) return set_error(CCT_ERR_ARG, "FP64 tracking needs segments");
     if (precision == 1 && (!d_packed || !aligned(d_packed, 256)))
         return set_error(CCT_ERR_ARG, "FP32c tracking needs a 256-byte aligned packed buffer");
     return launch_track(d_kls, d_p0s, d_seg_off, d_packed, d_qs, d_qs_off, n_designs, d_particles, n_particles,

@@ -13,7 +13,9 @@
 // never builds or copies segment arrays).  param_grad_kernel maps a segment gradient
 // dJ/d(kl_i, p0_i) to dJ/d(tilt angles, current, big_r) of each layer by forward-mode
 // differentiation of the same formulas, one CTA per layer with a fixed-order reduction.
+#include <algorithm>
 #include <cmath>
+#include <utility>
 #include <vector>
 
 #include "cctgpu_internal.cuh"
@@ -28,7 +30,7 @@ constexpr int kLayerParams = CCT_LAYER_PARAMS;
 enum : int {
     LR_ORIGIN = 0, LR_XI = 3, LR_YI = 6, LR_ZI = 9, LR_BIG_R = 12, LR_SMALL_R = 13, LR_CURRENT = 14,
     LR_KSI0 = 15, LR_PHI0 = 16, LR_KSI1 = 17, LR_PHI1 = 18, LR_WINDINGS = 19, LR_PER_WINDING = 20,
-    LR_NTILT = 21, LR_TILT = 22
+    LR_NTILT = 21, LR_TILT = 22, LR_FIRST = 30
 };
 
 struct LayerGeom {
@@ -102,12 +104,9 @@ __device__ __forceinline__ void to_global(const LayerGeom &G, double x, double y
                                            __dmul_rn(G.A[9 + c], z)));
 }
 
-// First segment of layer l: the layers' segments are concatenated in record order.
-__device__ int64_t layer_first_segment(const double *__restrict__ layers, int l) {
-    int64_t off = 0;
-    for (int i = 0; i < l; ++i)
-        off += (int64_t)layers[i * kLayerDoubles + LR_WINDINGS] * (int64_t)layers[i * kLayerDoubles + LR_PER_WINDING];
-    return off;
+// First segment of layer l in the segment arrays (record field 30).
+__device__ __forceinline__ int64_t layer_first_segment(const double *__restrict__ layers, int l) {
+    return (int64_t)layers[(int64_t)l * kLayerDoubles + LR_FIRST];
 }
 
 constexpr int kBuildBlock = 256;
@@ -226,12 +225,13 @@ __global__ void __launch_bounds__(kGradBlock) param_grad_kernel(const double *__
 
 // ------------------------------------------------------------------ host side
 static int check_layers(const double *h, int n_layers, int64_t *total) {
-    int64_t sum = 0;
+    std::vector<std::pair<int64_t, int64_t>> ranges;
+    ranges.reserve(n_layers);
     for (int l = 0; l < n_layers; ++l) {
         const double *r = h + (int64_t)l * kLayerDoubles;
         for (int i = 0; i < kLayerDoubles; ++i)
             if (!std::isfinite(r[i])) return set_error(CCT_ERR_ARG, "layer %d: field %d is not finite", l, i);
-        const double W = r[LR_WINDINGS], n = r[LR_PER_WINDING], nt = r[LR_NTILT];
+        const double W = r[LR_WINDINGS], n = r[LR_PER_WINDING], nt = r[LR_NTILT], f = r[LR_FIRST];
         if (W < 1 || W != std::floor(W) || n < 1 || n != std::floor(n) || W * n > 1e10)
             return set_error(CCT_ERR_ARG, "layer %d: winding number %g and segments per winding %g must be "
                                           "positive integers", l, W, n);
@@ -241,9 +241,18 @@ static int check_layers(const double *h, int n_layers, int64_t *total) {
             return set_error(CCT_ERR_ARG, "layer %d: need 0 <= small_r (%g) < big_r (%g)", l, r[LR_SMALL_R],
                              r[LR_BIG_R]);
         if (r[LR_KSI1] == r[LR_KSI0]) return set_error(CCT_ERR_ARG, "layer %d: xi start equals xi end", l);
-        sum += (int64_t)W * (int64_t)n;
+        if (f < 0 || f != std::floor(f) || f > 9e15)
+            return set_error(CCT_ERR_ARG, "layer %d: first segment %g must be a non-negative integer", l, f);
+        ranges.emplace_back((int64_t)f, (int64_t)f + (int64_t)W * (int64_t)n);
     }
-    *total = sum;
+    std::vector<std::pair<int64_t, int64_t>> sorted = ranges;
+    std::sort(sorted.begin(), sorted.end());
+    for (size_t i = 1; i < sorted.size(); ++i)
+        if (sorted[i].first < sorted[i - 1].second)
+            return set_error(CCT_ERR_ARG, "layers overlap in the segment arrays (segments %lld..%lld and %lld..%lld)",
+                             (long long)sorted[i - 1].first, (long long)sorted[i - 1].second,
+                             (long long)sorted[i].first, (long long)sorted[i].second);
+    *total = sorted.empty() ? 0 : sorted.back().second;
     return CCT_OK;
 }
 
@@ -256,9 +265,9 @@ static int fetch_and_check(const double *d_layers, int n_layers, int64_t n_seg, 
     int64_t total = 0;
     int rc = check_layers(h.data(), n_layers, &total);
     if (rc != CCT_OK) return rc;
-    if (total != n_seg)
-        return set_error(CCT_ERR_ARG, "the layers hold %lld segments, the buffers %lld", (long long)total,
-                         (long long)n_seg);
+    if (total > n_seg)
+        return set_error(CCT_ERR_ARG, "the layers reach segment %lld, the buffers hold %lld segments",
+                         (long long)total, (long long)n_seg);
     return CCT_OK;
 }
 
@@ -289,7 +298,7 @@ int cct_segments_build(const double *d_layers, int32_t n_layers, double *d_kls, 
     int sms = 0, dev = 0;
     CCT_TRY_CUDA(cudaGetDevice(&dev));
     CCT_TRY_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    const int64_t per_layer = (n_seg / n_layers + kBuildBlock - 1) / kBuildBlock;
+    const int64_t per_layer = (std::max<int64_t>(n_seg / n_layers, 1) + kBuildBlock - 1) / kBuildBlock;
     const int gx = (int)std::max<int64_t>(1, std::min<int64_t>(per_layer, 8 * (int64_t)sms));
     segments_build_kernel<<<dim3(gx, n_layers), kBuildBlock, 0, st>>>(d_layers, d_kls, d_p0s);
     CCT_TRY_CUDA(cudaGetLastError());

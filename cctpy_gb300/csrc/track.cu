@@ -179,6 +179,9 @@ static int run_track(const double *kls, const double *p0s, const int64_t *seg_of
     CCT_TRY_CUDA(cudaStreamSynchronize(st));
     for (int d = 0; d < n_designs; ++d)
         if (hoff[d + 1] < hoff[d]) return set_error(CCT_ERR_ARG, "segment offsets decrease at design %d", d);
+    if (precision == 0 && hoff[n_designs] > hoff[0] && (!kls || !p0s))
+        return set_error(CCT_ERR_ARG, "FP64 tracking of %lld segments needs d_kls and d_p0s",
+                         (long long)(hoff[n_designs] - hoff[0]));
     const unsigned char *tiles = nullptr;
     const int64_t *tile_off = nullptr;
     if (precision == 1) {
@@ -282,6 +285,10 @@ __global__ void plan_kernel(TrackParams P, const unsigned char *packed, int64_t 
             return;
         }
         tiles_total += tiles_of(P.seg_off, d);
+    }
+    if (P.precision == 0 && P.seg_off[P.n_designs] > P.seg_off[0] && (!P.kls || !P.p0s)) {
+        atomicExch(err, (unsigned)CCT_ERR_ARG);
+        return;
     }
     if (P.precision == 1) {
         const int64_t *h = reinterpret_cast<const int64_t *>(packed);
@@ -406,7 +413,6 @@ extern "C" int cct_track_async(const double *d_kls, const double *d_p0s, const i
     if (n_designs <= 0 || n_particles <= 0) return set_error(CCT_ERR_ARG, "need at least one design and particle");
     if (!d_seg_off || !d_particles || !d_scratch) return set_error(CCT_ERR_ARG, "null offsets, particles or scratch");
     if (precision != 0 && precision != 1) return set_error(CCT_ERR_ARG, "precision must be 0 (FP64) or 1 (FP32c)");
-    if (precision == 0 && (!d_kls || !d_p0s)) return set_error(CCT_ERR_ARG, "FP64 tracking needs d_kls and d_p0s");
     if (precision == 1 && !d_packed) return set_error(CCT_ERR_ARG, "FP32c tracking needs the packed segments");
     if (!(distance >= 0.0) || !(footstep > 0.0)) return set_error(CCT_ERR_ARG, "distance >= 0 and footstep > 0 needed");
     return launch_track_async(d_kls, d_p0s, d_seg_off, d_packed, d_qs, d_qs_off, n_designs, d_particles, n_particles,
@@ -579,7 +585,6 @@ extern "C" int cct_track_static_scratch(const double *d_kls, const double *d_p0s
         return set_error(CCT_ERR_ARG, "distance (%g) and footstep (%g) must be positive", distance, footstep);
     if (precision != 0 && precision != 1) return set_error(CCT_ERR_ARG, "precision must be 0 or 1");
     if (!d_seg_off || !d_qs_off || !d_particles) return set_error(CCT_ERR_ARG, "null pointer");
-    if (precision == 0 && (!d_kls || !d_p0s)) return set_error(CCT_ERR_ARG, "FP64 tracking needs segments");
     if (precision == 1 && (!d_packed || reinterpret_cast<uintptr_t>(d_packed) % 256))
         return set_error(CCT_ERR_ARG, "FP32c tracking needs a 256-byte aligned packed buffer");
     return launch_track_static(d_kls, d_p0s, d_seg_off, d_packed, d_qs, d_qs_off, n_designs, d_particles,

@@ -10,7 +10,7 @@ form is built on first use.  Torch provides device memory and the stream.
 from __future__ import annotations
 
 import ctypes
-from typing import List, Sequence
+from typing import List, Optional, Sequence
 
 import numpy as np
 import torch
@@ -35,14 +35,24 @@ def _stream() -> int:
 
 
 def _classify(m):
-    """'cct' / 'qs' for magnets the kernels evaluate (this package's classes or any object
-    with cctpy's CCT / QS attributes); raises ValueError otherwise, as cctpy's GPU path does
-    (gpu_accelerator.py:1969-1970)."""
+    """The kind of a magnet the kernels evaluate (this package's classes or any object with
+    cctpy's attributes): 'cct' (winding segments), 'qs', 'q', 'lum' (LocalUniformMagnet),
+    'uniform' (UniformMagnet) -- analytic records --, 'wire' (Wire, AGCCT_CONNECTOR: current
+    elements).  Raises ValueError otherwise."""
     if hasattr(m, "winding_number") and hasattr(m, "tilt_angles") and hasattr(m, "local_coordinate_system"):
         return "cct"
     if hasattr(m, "second_gradient") and hasattr(m, "aperture_radius") and hasattr(m, "local_coordinate_system"):
         return "qs"
-    raise ValueError(f"magnet {m} cannot be evaluated on the GPU (only CCT and QS are supported)")
+    if hasattr(m, "magnetic_field") and hasattr(m, "aperture_radius") and hasattr(m, "local_coordinate_system"):
+        return "lum"
+    if hasattr(m, "gradient") and hasattr(m, "aperture_radius") and hasattr(m, "local_coordinate_system"):
+        return "q"
+    if hasattr(m, "elementary_current") and hasattr(m, "elementary_current_position") and hasattr(m, "current"):
+        return "wire"
+    if hasattr(m, "magnetic_field") and hasattr(getattr(m, "magnetic_field"), "x"):
+        return "uniform"
+    raise ValueError(f"magnet {m} cannot be evaluated on the GPU (CCT, QS, Q, LocalUniformMagnet, UniformMagnet, "
+                     "Wire and AGCCT_CONNECTOR are supported)")
 
 
 def magnet_list(obj) -> List:
@@ -74,6 +84,68 @@ def qs_record(m) -> np.ndarray:
     return np.asarray(m.to_numpy_array(np.float64), dtype=np.float64)
 
 
+def _frame12(lcs) -> List[float]:
+    return _xyz(lcs.location) + _xyz(lcs.XI) + _xyz(lcs.YI) + _xyz(lcs.ZI)
+
+
+def analytic_record(m) -> Optional[np.ndarray]:
+    """16-double record of an analytic magnet, or None if it contributes no field.
+    QS: QS.to_numpy_array (magnets.py:726-748).  Q: the same with no sextupole term
+    (magnets.py:762-801).  LocalUniformMagnet: frame, -length, field, 0, aperture (a negative
+    length marks the uniform-field kind; magnets.py:440-481).  UniformMagnet: a frame whose YI
+    is the field direction, length -inf (everywhere), |B| (magnets.py:417-437)."""
+    kind = _classify(m)
+    if kind == "qs":
+        return qs_record(m)
+    if kind == "q":
+        return np.array(_frame12(m.local_coordinate_system) + [m.length, m.gradient, 0.0, m.aperture_radius])
+    if kind == "lum":
+        if not m.length > 0:
+            return None
+        return np.array(_frame12(m.local_coordinate_system) + [-float(m.length), float(m.magnetic_field), 0.0,
+                                                                 float(m.aperture_radius)])
+    if kind == "uniform":
+        b = np.array(_xyz(m.magnetic_field))
+        n = float(np.sqrt(b @ b))
+        if n == 0.0:
+            return None
+        y = b / n
+        helper = np.array([1.0, 0.0, 0.0]) if abs(y[0]) < 0.9 else np.array([0.0, 1.0, 0.0])
+        x = np.cross(y, helper)
+        x /= np.sqrt(x @ x)
+        z = np.cross(x, y)
+        return np.concatenate([[0.0, 0.0, 0.0], x, y, z, [-np.inf, n, 0.0, np.inf]])
+    raise ValueError(f"{m} is not an analytic magnet")
+
+
+def wire_segments(m) -> Optional[tuple]:
+    """(kl, p0) global (N, 3) current elements of a Wire (global path, cct.py:625-691) or an
+    AGCCT_CONNECTOR (local path, moved to the global frame; cct.py:835-994), or None if it
+    carries no current."""
+    if approx_zero(float(m.current)):
+        return None
+    if hasattr(m, "start") and hasattr(m, "end") and not hasattr(m, "local_coordinate_system"):
+        if _approx_equal(float(m.start), float(m.end)):
+            return None
+    kl = np.asarray(m.elementary_current, dtype=np.float64).reshape(-1, 3)
+    p0 = np.asarray(m.elementary_current_position, dtype=np.float64).reshape(-1, 3)
+    lcs = getattr(m, "local_coordinate_system", None)
+    if lcs is not None:
+        R = np.array([_xyz(lcs.XI), _xyz(lcs.YI), _xyz(lcs.ZI)])
+        o = np.array(_xyz(lcs.location))
+        kl = kl @ R
+        p0 = o + p0 @ R
+    return np.ascontiguousarray(kl), np.ascontiguousarray(p0)
+
+
+def _approx_equal(a: float, b: float, err: float = 1e-6) -> bool:
+    return a == b or abs(a - b) <= err or ((a + b != 0.0) and 2 * abs((a - b) / (a + b)) <= err)
+
+
+def approx_zero(v: float) -> bool:
+    return _approx_equal(v, 0.0)
+
+
 LAYER_DOUBLES, LAYER_MAX_TILTS, LAYER_PARAMS = 32, 8, 10
 
 
@@ -81,10 +153,10 @@ def _xyz(p) -> List[float]:
     return [float(p.x), float(p.y), float(p.z)]
 
 
-def layer_record(m) -> np.ndarray:
+def layer_record(m, first: int = 0) -> np.ndarray:
     """The 32-double layer record of a CCT (ours or cctpy's) that cct_segments_build reads:
     frame (origin, XI, YI, ZI), big_r, small_r, current, xi/phi start and end, winding number,
-    segments per winding, tilt count and tilt angles (degrees)."""
+    segments per winding, tilt count, tilt angles (degrees), index of its first segment."""
     lcs = m.local_coordinate_system
     tilts = [float(t) for t in m.tilt_angles]
     if len(tilts) > LAYER_MAX_TILTS:
@@ -95,28 +167,39 @@ def layer_record(m) -> np.ndarray:
     r[12:22] = [m.big_r, m.small_r, m.current, s.x, s.y, e.x, e.y, m.winding_number,
                 m.disperse_number_per_winding, len(tilts)]
     r[22:22 + len(tilts)] = tilts
+    r[30] = first
     return r
 
 
 def device_layers(magnets: Sequence) -> tuple:
-    """(layer records, CCT magnets, QS records (m, 16)) of one design, with the CCT layers in
-    host_design's order (zero-current layers dropped)."""
-    recs, ccts, qss = [], [], []
+    """(layer records, CCT magnets, analytic records (m, 16), other current elements (kl, p0)
+    or None) of one design, with the CCT layers in host_design's order (zero-current layers
+    dropped)."""
+    recs, ccts, ana, wires = [], [], [], []
     for m in magnets:
-        if _classify(m) == "cct":
+        kind = _classify(m)
+        if kind == "cct":
             if abs(float(m.current)) <= 1e-6:
                 continue
             recs.append(layer_record(m))
             ccts.append(m)
+        elif kind == "wire":
+            w = wire_segments(m)
+            if w is not None:
+                wires.append(w)
         else:
-            qss.append(qs_record(m))
-    return recs, ccts, (np.stack(qss) if qss else np.zeros((0, 16)))
+            r = analytic_record(m)
+            if r is not None:
+                ana.append(r)
+    extra = (np.concatenate([w[0] for w in wires]), np.concatenate([w[1] for w in wires])) if wires else None
+    return recs, ccts, (np.stack(ana) if ana else np.zeros((0, 16))), extra
 
 
 def host_design(magnets: Sequence) -> tuple:
-    """(kls (N,3), p0s (N,3), qs (M,16)) of one design.  A CCT with |current| <= 1e-6
-    contributes nothing (cct.py:254-255)."""
-    kls, p0s, qss = [], [], []
+    """(kls (N,3), p0s (N,3), analytic records (M,16)) of one design: the CCT layers' segments
+    in magnet order, then the current elements of wires and connectors.  A CCT with
+    |current| <= 1e-6 contributes nothing (cct.py:254-255)."""
+    kls, p0s, ana, wkl, wp0 = [], [], [], [], []
     for m in magnets:
         kind = _classify(m)
         if kind == "cct":
@@ -125,11 +208,20 @@ def host_design(magnets: Sequence) -> tuple:
             kl, p0 = cct_global_segments(m)
             kls.append(kl)
             p0s.append(p0)
+        elif kind == "wire":
+            w = wire_segments(m)
+            if w is not None:
+                wkl.append(w[0])
+                wp0.append(w[1])
         else:
-            qss.append(qs_record(m))
+            r = analytic_record(m)
+            if r is not None:
+                ana.append(r)
+    kls += wkl
+    p0s += wp0
     kl = np.concatenate(kls) if kls else np.zeros((0, 3))
     p0 = np.concatenate(p0s) if p0s else np.zeros((0, 3))
-    qs = np.stack(qss) if qss else np.zeros((0, 16))
+    qs = np.stack(ana) if ana else np.zeros((0, 16))
     return np.ascontiguousarray(kl), np.ascontiguousarray(p0), np.ascontiguousarray(qs)
 
 
@@ -165,18 +257,32 @@ class DesignSet:
             self.layers = self.h_layers = self.layer_design = None
 
     @classmethod
-    def from_layers(cls, layer_lists: Sequence[Sequence[np.ndarray]], qs_lists: Sequence[np.ndarray]) -> "DesignSet":
-        """Design set whose segments are generated on the device from CCT layer records
-        (`layer_record`): layer_lists[d] = records of design d, qs_lists[d] = (m, 16)."""
+    def from_layers(cls, layer_lists: Sequence[Sequence[np.ndarray]], qs_lists: Sequence[np.ndarray],
+                    extra_segments: Sequence = None) -> "DesignSet":
+        """Design set whose CCT segments are generated on the device from layer records
+        (`layer_record`): layer_lists[d] = records of design d, qs_lists[d] = (m, 16) analytic
+        records, extra_segments[d] = None or (kl, p0) global current elements of the design's
+        wires and connectors (placed after its layers)."""
         lib = _lib.load()
         dev = _device()
         self = cls.__new__(cls)
-        recs = [r for ls in layer_lists for r in ls]
+        extra = extra_segments or [None] * len(layer_lists)
+        recs, seg_counts, at = [], [], 0
+        self.layer_design = []
+        for d, ls in enumerate(layer_lists):
+            start = at
+            for r in ls:                                   # layers first, in order
+                r = np.array(r, dtype=np.float64)
+                r[30] = at
+                recs.append(r)
+                self.layer_design.append(d)
+                at += int(r[19]) * int(r[20])
+            if extra[d] is not None:                       # then the design's other current elements
+                at += int(extra[d][0].shape[0])
+            seg_counts.append(at - start)
+        self.layer_design = np.array(self.layer_design, dtype=np.int64)
         self.h_layers = np.ascontiguousarray(np.stack(recs) if recs else np.zeros((0, LAYER_DOUBLES)))
-        self.layer_design = np.array([d for d, ls in enumerate(layer_lists) for _ in ls], dtype=np.int64)
-        counts = [int(r[19]) * int(r[20]) for r in recs]
-        seg_counts = [sum(counts[i] for i in np.nonzero(self.layer_design == d)[0]) for d in range(len(layer_lists))]
-        n = int(sum(counts))
+        n = at
         if recs:
             total = lib.cct_layer_segments(self.h_layers.ctypes.data_as(ctypes.c_void_p), len(recs))
             _lib.check(0 if total >= 0 else _lib.CCT_ERR_ARG, "cct_layer_segments")
@@ -186,6 +292,14 @@ class DesignSet:
         if recs:
             _lib.check(lib.cct_segments_build(_ptr(self.layers), len(recs), _ptr(kls), _ptr(p0s), n, _stream()),
                        "cct_segments_build")
+        at = 0
+        for d, ls in enumerate(layer_lists):
+            at += sum(int(r[19]) * int(r[20]) for r in ls)
+            if extra[d] is not None:
+                k = int(extra[d][0].shape[0])
+                kls[at:at + k] = torch.as_tensor(extra[d][0], dtype=torch.float64, device=dev)
+                p0s[at:at + k] = torch.as_tensor(extra[d][1], dtype=torch.float64, device=dev)
+                at += k
         self._finish(seg_counts, [np.asarray(q, dtype=np.float64).reshape(-1, 16) for q in qs_lists], kls, p0s)
         return self
 
@@ -247,7 +361,7 @@ def design_set_of(objs: Sequence, segments: str = "host") -> DesignSet:
     if segments != "device":
         raise ValueError(f"segments must be 'host' or 'device', not {segments!r}")
     parts = [device_layers(magnet_list(o)) for o in objs]
-    ds = DesignSet.from_layers([p[0] for p in parts], [p[2] for p in parts])
+    ds = DesignSet.from_layers([p[0] for p in parts], [p[2] for p in parts], [p[3] for p in parts])
     ds.layer_magnets = [m for p in parts for m in p[1]]
     return ds
 

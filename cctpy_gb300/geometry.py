@@ -9,7 +9,7 @@ numpy transforms for segment sets.
 from __future__ import annotations
 
 import math
-from typing import List, Optional, Union
+from typing import Callable, List, Optional, Tuple, Union
 
 import numpy as np
 
@@ -299,6 +299,30 @@ class Line2:
     def direct_at_end(self) -> P2:
         return self.direct_at(self.get_length())
 
+    def disperse2d(self, step: float = 1.0 * MM) -> List[P2]:
+        """Points at ceil(length / step) + 1 equally spaced arc lengths (line2s.py:190-205)."""
+        number = int(math.ceil(self.get_length() / step)) + 1
+        return [self.point_at(s) for s in linspace(0, self.get_length(), number)]
+
+
+def approx_equal(a: float, b: float, err: float = 1e-6) -> bool:
+    """BaseUtils.equal for numbers (base_utils.py:35-58)."""
+    return a == b or abs(a - b) <= err or ((a + b != 0.0) and 2 * abs((a - b) / (a + b)) <= err)
+
+
+def linspace(start, end, number: int) -> list:
+    """BaseUtils.linspace (base_utils.py:81-90): d = (end - start) * (1 / (number - 1)),
+    start + d * float(i)."""
+    d = (end - start) * (1 / (number - 1))
+    return [start + d * float(i) for i in range(number)]
+
+
+def derivative(func: Callable, delta: float = 1e-7) -> Callable:
+    """BaseUtils.derivative (base_utils.py:194-203): central difference of step delta."""
+    def d(x):
+        return (func(x + delta / 2) - func(x - delta / 2)) / delta
+    return d
+
 
 class StraightLine2(Line2):
     def __init__(self, length: float, direct: P2, start_point: P2):
@@ -314,6 +338,43 @@ class StraightLine2(Line2):
 
     def direct_at(self, s: float) -> P2:
         return self.direct
+
+    def straight_line_equation(self) -> Tuple[float, float, float]:
+        """A, B, C of A x + B y + C = 0 through the start and start + direct
+        (line2s.py:330-365)."""
+        if approx_equal(self.direct.length(), 0, err=1e-10):
+            raise ValueError("straight_line_equation: the direction has zero length")
+        x1, y1 = self.start_point.x, self.start_point.y
+        e = self.direct + self.start_point
+        x2, y2 = e.x, e.y
+        if approx_equal(x1, x2, err=1e-10):
+            return 1.0, 0.0, -x1
+        if approx_equal(y1, y2, err=1e-10):
+            return 0.0, 1.0, -y1
+        return (y2 - y1), (x1 - x2), (x2 * y1 - x1 * y2)
+
+    @staticmethod
+    def intersecting_point(pa: P2, va: P2, pb: P2, vb: P2) -> Tuple[P2, float, float]:
+        """Intersection cp of the lines pa + ka va and pb + kb vb, with ka and kb
+        (line2s.py:368-412)."""
+        if approx_equal(va.length(), 0.0, err=1e-10) or approx_equal(vb.length(), 0.0, err=1e-10):
+            raise ValueError(f"intersecting_point: a direction has zero length (va={va}, vb={vb})")
+        A1, B1, C1 = StraightLine2(1.0, va, pa).straight_line_equation()
+        A2, B2, C2 = StraightLine2(1.0, vb, pb).straight_line_equation()
+        cpy = (A1 * C2 - A2 * C1) / (A2 * B1 - A1 * B2)
+        cpx = -(B1 * cpy + C1) / A1 if A1 != 0 else -(B2 * cpy + C2) / A2
+        cp = P2(cpx, cpy)
+        ka = (cp.x - pa.x) / va.x if va.x != 0 else (cp.y - pa.y) / va.y
+        kb = (cp.x - pb.x) / vb.x if vb.x != 0 else (cp.y - pb.y) / vb.y
+        return cp, ka, kb
+
+    @staticmethod
+    def is_on_right(view_point: P2, view_direct: P2, viewed_point: P2) -> int:
+        """1 if viewed_point is on the right of the view direction, -1 left, 0 ahead or
+        behind (line2s.py:414-434)."""
+        right = view_direct.copy().rotate(-90 / 180.0 * math.pi)
+        k = right * (viewed_point - view_point)
+        return 1 if k > 0 else (-1 if k < 0 else 0)
 
     def side_of(self, p: P2) -> int:
         """+1 if p lies on the right of the directed line, -1 on the left, 0 on it (1e-6)."""
@@ -425,3 +486,32 @@ def circle_center_and_radius(p1: P2, p2: P2, p3: P2):
     cx, cy = float(c[0, 0]), float(c[1, 0])
     r = sum(math.sqrt((cx - x) ** 2 + (cy - y) ** 2) for x, y in zip(xs, ys)) / 3
     return P2(cx, cy), r
+
+
+class FunctionLine3:
+    """A 3-D curve p = f(s), s from start to end (cctpy line3s.py:166-264)."""
+
+    def __init__(self, p3_function: Callable[[float], P3], start: float, end: float,
+                 direct_function: Optional[Callable[[float], P3]] = None, delta_for_disperse: float = 1 * MM,
+                 delta_for_compute_direct_function: float = 0.1 * MM):
+        self._f = p3_function
+        self._start, self._end = start, end
+        if direct_function is None:
+            def direct_function(t):
+                return (self._f(t + delta_for_compute_direct_function) - self._f(t)) / delta_for_compute_direct_function
+        self._direct = direct_function
+
+    def point_at_p3_function(self, s: float) -> P3:
+        return self._f(s)
+
+    def direct_at_p3_function(self, s: float) -> P3:
+        return self._direct(s)
+
+    def get_start(self) -> float:
+        return self._start
+
+    def get_end(self) -> float:
+        return self._end
+
+    def get_p3_function(self) -> Callable[[float], P3]:
+        return self._f

@@ -8,11 +8,12 @@ vectorised numpy in FP64.
 from __future__ import annotations
 
 import math
-from typing import Iterable, List, Tuple
+from typing import Iterable, List, Optional, Tuple
 
 import numpy as np
 
-from .geometry import MM, P2, P3, LocalCoordinateSystem, StraightLine2, Trajectory, as_xyz, circle_center_and_radius
+from .geometry import (MM, FunctionLine3, P2, P3, LocalCoordinateSystem, StraightLine2, Trajectory, approx_equal,
+                       as_xyz, circle_center_and_radius, derivative, linspace)
 
 
 def _deg2rad(d: float) -> float:
@@ -176,6 +177,30 @@ class CCT(Magnet):
                 phi = phi + ((1 / math.tan(self.tilt_radians[i])) / ((i + 1) * sh)) * np.sin((i + 1) * ksi)
         return phi
 
+    def phi_at(self, ksi: float) -> float:
+        """phi(xi) for one xi with the math module, term by term as cct.py:166-188."""
+        x1, y1 = self.starting_point_in_ksi_phi_coordinate.x, self.starting_point_in_ksi_phi_coordinate.y
+        x2, y2 = self.end_point_in_ksi_phi_coordinate.x, self.end_point_in_ksi_phi_coordinate.y
+        k = (y2 - y1) / (x2 - x1)
+        b = -k * x1 + y1
+        phi = k * ksi + b
+        for i, t in enumerate(self.tilt_angles):
+            if not _is_90(t):
+                phi += (1 / math.tan(self.tilt_radians[i])) / ((i + 1) * math.sinh(self.eta)) * math.sin((i + 1) * ksi)
+        return phi
+
+    def p2_function(self, ksi: float) -> P2:
+        """(xi, phi(xi)) (cct.py:459-465)."""
+        return P2(ksi, self.phi_at(ksi))
+
+    def p3_function(self, ksi: float) -> P3:
+        """Winding point at xi in the local frame (cct.py:467-473 with the bipolar-toroidal
+        conversion of :213-224)."""
+        phi = self.phi_at(ksi)
+        temp = self.a / (math.cosh(self.eta) - math.cos(ksi))
+        return P3(temp * math.sinh(self.eta) * math.cos(phi), temp * math.sinh(self.eta) * math.sin(phi),
+                  temp * math.sin(ksi))
+
     def ksi_samples(self) -> np.ndarray:
         x1, x2 = self.starting_point_in_ksi_phi_coordinate.x, self.end_point_in_ksi_phi_coordinate.x
         n = self.total_disperse_number
@@ -261,3 +286,161 @@ class CCT(Magnet):
                 f"small_r({self.small_r})bending_angle({self.bending_angle})tilt_angles({self.tilt_angles})"
                 f"winding_number({self.winding_number})current({self.current})"
                 f"disperse_number_per_winding({self.disperse_number_per_winding})")
+
+
+
+class Q(Magnet):
+    """Hard-edge quadrupole: a QS without the sextupole term (magnets.py:762-832)."""
+
+    def __init__(self, local_coordinate_system: LocalCoordinateSystem, length: float, gradient: float,
+                 aperture_radius: float):
+        self.local_coordinate_system = local_coordinate_system
+        self.length = float(length)
+        self.gradient = float(gradient)
+        self.aperture_radius = float(aperture_radius)
+        self.qs = QS(local_coordinate_system, length, gradient, 0.0, aperture_radius)
+
+    def is_out_of_aperture(self, point: P3) -> bool:
+        return self.qs.is_out_of_aperture(point)
+
+    @staticmethod
+    def create_q_along(trajectory, s: float, length: float, gradient: float, aperture_radius: float) -> "Q":
+        origin = trajectory.point_at(s)
+        z = trajectory.direct_at(s)
+        x = z.rotate(_deg2rad(90))
+        return Q(LocalCoordinateSystem(origin.to_p3(), x.to_p3(), z.to_p3()), length, gradient, aperture_radius)
+
+    @staticmethod
+    def as_q(anything) -> "Q":
+        return anything
+
+    def __repr__(self) -> str:
+        return (f"Q:local_coordinate_system={self.local_coordinate_system}, length={self.length}, "
+                f"gradient={self.gradient}, aperture_radius={self.aperture_radius}")
+
+
+class LocalUniformMagnet(Magnet):
+    """Uniform field `magnetic_field` (tesla) along the frame's YI inside the cylinder of radius
+    aperture_radius around ZI for 0 <= z <= length, zero outside: a straight dipole
+    (magnets.py:440-536)."""
+
+    def __init__(self, local_coordinate_system: LocalCoordinateSystem, length: float, aperture_radius: float,
+                 magnetic_field: float):
+        self.local_coordinate_system = local_coordinate_system
+        self.length = float(length)
+        self.aperture_radius = float(aperture_radius)
+        self.magnetic_field = float(magnetic_field)
+        self.magnetic_field_vector = local_coordinate_system.YI * self.magnetic_field
+
+    def is_out_of_aperture(self, point: P3) -> bool:
+        lp = self.local_coordinate_system.point_to_local_coordinate(point)
+        if lp.z < 0 or lp.z > self.length:
+            return True
+        a = self.aperture_radius
+        return abs(lp.x) > a or abs(lp.y) > a or math.sqrt(lp.x ** 2 + lp.y ** 2) > a
+
+    @staticmethod
+    def create_local_uniform_magnet_along(trajectory, s: float, magnetic_field: float, length: float,
+                                          aperture_radius: float) -> "LocalUniformMagnet":
+        origin = trajectory.point_at(s)
+        z = trajectory.direct_at(s)
+        x = z.rotate(_deg2rad(90))
+        return LocalUniformMagnet(LocalCoordinateSystem(origin.to_p3(), x.to_p3(), z.to_p3()), length,
+                                  aperture_radius, magnetic_field)
+
+
+class UniformMagnet(Magnet):
+    """The same field everywhere (magnets.py:417-437)."""
+
+    def __init__(self, magnetic_field: P3 = None):
+        self.magnetic_field = P3() if magnetic_field is None else magnetic_field
+
+
+class Wire(Magnet):
+    """A wire along a 3-D curve in the global frame, cut into straight current elements of
+    about delta_length in the curve's parameter (cct.py:625-691)."""
+
+    def __init__(self, function_line3: FunctionLine3, current: float, delta_length: float = 1 * MM):
+        self.function_line3 = function_line3
+        self.current = current
+        self.start = function_line3.get_start()
+        self.end = function_line3.get_end()
+        part_number = int(math.ceil((self.end - self.start) / delta_length))
+        if part_number < 1:
+            raise ValueError(f"a wire from {self.start} to {self.end} has no current element (the curve parameter "
+                             "must increase)")
+        self.dispersed_s = np.array(linspace(self.start, self.end, part_number + 1))
+        self.dispersed_path3 = np.array([function_line3.point_at_p3_function(t).to_numpy_ndarry3()
+                                         for t in self.dispersed_s])
+        p = self.dispersed_path3
+        self.elementary_current = 1e-7 * self.current * (p[1:] - p[:-1])
+        self.elementary_current_position = 0.5 * (p[1:] + p[:-1])
+
+    @staticmethod
+    def create_by_cct(cct: "CCT") -> "Wire":
+        """The CCT's winding as a wire (cct.py:814-832; the path is the CCT's local one)."""
+        return Wire(FunctionLine3(cct.p3_function, cct.starting_point_in_ksi_phi_coordinate.x,
+                                  cct.end_point_in_ksi_phi_coordinate.x),
+                    cct.current, cct.small_r * _deg2rad(360 / cct.winding_number))
+
+
+class AGCCT_CONNECTOR(Magnet):
+    """The winding joining two consecutive AG-CCT layers of one frame (cct.py:835-994): in the
+    plane (z, Xi) = (phi R, xi r) a straight run and a half circle from the first layer's end
+    to the second layer's start, along the tangents of the two windings there, cut into
+    `step` pieces and mapped back to the torus.  Current elements in the layers' local frame."""
+
+    def __init__(self, agcct1: "CCT", agcct2: "CCT", step: float = 1 * MM):
+        lcs1, lcs2 = agcct1.local_coordinate_system, agcct2.local_coordinate_system
+        if not (lcs1.location == lcs2.location and lcs1.XI == lcs2.XI and lcs1.YI == lcs2.YI
+                and lcs1.ZI == lcs2.ZI):
+            raise ValueError(f"the CCTs to connect are not in one frame: {agcct1}, {agcct2}")
+        for what, u, v in (("big_r", agcct1.big_r, agcct2.big_r), ("small_r", agcct1.small_r, agcct2.small_r),
+                           ("current", agcct1.current, agcct2.current)):
+            if not approx_equal(u, v):
+                raise ValueError(f"the CCTs to connect differ in {what}: {u} != {v}")
+        pre_end, next_start = agcct1.end_point_in_ksi_phi_coordinate, agcct2.starting_point_in_ksi_phi_coordinate
+        if not approx_equal(pre_end.x, next_start.x):
+            raise ValueError(f"the first CCT ends at xi = {pre_end.x}, the second starts at xi = {next_start.x}")
+        self.current = agcct1.current
+        self.local_coordinate_system = lcs1
+        a = P2(x=pre_end.y * agcct1.big_r, y=0.0)
+        b = P2(x=next_start.y * agcct2.big_r, y=0.0)
+
+        def tangent(c):
+            sign = -1 if c.starting_point_in_ksi_phi_coordinate.x > c.end_point_in_ksi_phi_coordinate.x else 1
+            f = derivative(lambda ksi: P2(x=c.p2_function(ksi).y * c.big_r, y=c.p2_function(ksi).x * c.small_r))
+            return f, sign
+
+        fa, sa = tangent(agcct1)
+        fb, sb = tangent(agcct2)
+        va = fa(pre_end.x) * sa
+        vb = fb(next_start.x) * sb
+        ip, ka, kb = StraightLine2.intersecting_point(pa=a, va=va.copy().rotate(_deg2rad(90)), pb=b, vb=vb)
+        if kb > 0:
+            ip, ka, kb = StraightLine2.intersecting_point(pa=a, va=va, pb=b, vb=vb.copy().rotate(_deg2rad(90)))
+            if ka < 0:
+                raise ValueError("AGCCT_CONNECTOR: the tangents of the two windings do not meet ahead")
+            ca = a + ka * va
+            line = (Trajectory.set_start_point(a).first_line(direct=va, length=abs(ka * va.length()))
+                    .add_arc_line(radius=(ca - b).length() / 2,
+                                  clockwise=StraightLine2.is_on_right(ca, va, b) == 1, angle_deg=180.0))
+        else:
+            cb = b + kb * vb
+            line = (Trajectory.set_start_point(a).first_line(direct=va, length=0.0)
+                    .add_arc_line(radius=(a - cb).length() / 2, clockwise=StraightLine2.is_on_right(a, va, b) == 1,
+                                  angle_deg=180.0)
+                    .add_strait_line(length=abs(kb * vb.length())))
+        self.connector_line_in_z_Θ = line
+        self.length_in_z_Θ = line.get_length()
+        r, R = agcct1.small_r, agcct1.big_r
+        pts = []
+        for p2 in line.disperse2d(step=step):
+            ksi, phi = p2.y / r, p2.x / R
+            temp = agcct1.a / (math.cosh(agcct1.eta) - math.cos(ksi))
+            pts.append([temp * math.sinh(agcct1.eta) * math.cos(phi), temp * math.sinh(agcct1.eta) * math.sin(phi),
+                        temp * math.sin(ksi)])
+        self.dispersed_path3 = np.array(pts)
+        p = self.dispersed_path3
+        self.elementary_current = 1e-7 * self.current * (p[1:] - p[:-1])
+        self.elementary_current_position = 0.5 * (p[1:] + p[:-1])

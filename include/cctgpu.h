@@ -18,8 +18,15 @@
  *              each design's first segment.
  *   QS         d_qs[n_qs*16], FP64: origin, XI, YI, ZI, length, gradient,
  *              second gradient, aperture radius -- QS.to_numpy_array
- *              (cctpy final_code/packages/magnets.py:726-748).  Per design
- *              ranges in d_qs_off[n_designs+1].
+ *              (cctpy final_code/packages/magnets.py:726-748); a Q is a QS
+ *              without second gradient.  The same records also carry the
+ *              straight dipole (LocalUniformMagnet, magnets.py:440-481) as
+ *              origin, XI, YI, ZI, -length, field (T, along YI), 0, aperture
+ *              radius -- a negative length marks it -- and the uniform field
+ *              (UniformMagnet, :417-437) as length -inf with the field along
+ *              YI.  Per design ranges in d_qs_off[n_designs+1].  Wires and
+ *              AG-CCT connectors (cct.py:625-994) are current elements: their
+ *              kl/p0 go into the segment arrays like a CCT's.
  *   points     d_points[n*3] FP64 global xyz; fields d_B[n*3] FP64 tesla.
  *   particles  d_particles[n_designs*n_particles*10] FP64 records
  *              (px,py,pz,vx,vy,vz,relativistic mass,charge,speed,distance),
@@ -226,20 +233,22 @@ int cct_track_static_scratch(const double *d_kls, const double *d_p0s,
  *        (starting/end_point_in_ksi_phi_coordinate)
  *   [19] winding number  [20] segments per winding
  *   [21] number of tilt angles (0..CCT_LAYER_MAX_TILTS)
- *   [22..29] tilt angles in degrees  [30..31] unused (0)
- * Layer l owns winding_number * segments_per_winding segments, the layers'
- * segments concatenated in record order (a design set lists its designs'
- * layers one design after the other, as cct_track's segment offsets expect).
+ *   [22..29] tilt angles in degrees
+ *   [30] index of the layer's first segment in d_kls / d_p0s  [31] unused (0)
+ * Layer l owns winding_number * segments_per_winding segments from its first
+ * one on; layers must not overlap, and segments no layer covers (a wire's or a
+ * connector's current elements, filled by the caller) are left untouched.
  * Values agree with the host construction to rounding of the trigonometric
- * functions (about 1e-13 relative in kl).  Both calls read the records back to
- * check them (CCT_ERR_ARG on a bad record or a segment count other than
- * n_seg) and are synchronous.
+ * functions (winding points within about 2e-14 m).  Both calls read the records
+ * back to check them (CCT_ERR_ARG on a bad record, overlapping layers, or a
+ * layer reaching past n_seg) and are synchronous.
  * ------------------------------------------------------------------------- */
 #define CCT_LAYER_DOUBLES 32
 #define CCT_LAYER_MAX_TILTS 8
 #define CCT_LAYER_PARAMS 10
 
-/* Total segment count of host layer records (-1 and an error on a bad record). */
+/* End (one past the last segment) of the furthest of the host layer records;
+ * -1 and an error on a bad record or overlapping layers. */
 int64_t cct_layer_segments(const double *h_layers, int32_t n_layers);
 
 /* Writes d_kls[n_seg*3], d_p0s[n_seg*3] (global frame, FP64) of the layers in

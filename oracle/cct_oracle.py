@@ -396,6 +396,37 @@ class QSOracle:
                            + [r["length"], r["gradient"], r["second_gradient"], r["aperture_radius"]])
 
 
+class LocalUniformOracle:
+    """LocalUniformMagnet.magnetic_field_at, magnets.py:469-481: YI * B inside the cylinder."""
+
+    def __init__(self, frame: Frame, length: float, aperture_radius: float, field: float):
+        self.frame, self.length, self.a, self.b = frame, length, aperture_radius, field
+        self.vector = v3_scale(frame.YI, field)
+
+    def field_at(self, point: V3) -> V3:
+        x, y, z = self.frame.point_to_local(point)
+        if z < 0 or z > self.length:
+            return (0.0, 0.0, 0.0)
+        if abs(x) > self.a or abs(y) > self.a or math.sqrt(x ** 2 + y ** 2) > self.a:
+            return (0.0, 0.0, 0.0)
+        return self.vector
+
+
+class SegmentsOracle:
+    """Current elements (kl, p0): a Wire in the global frame (cct.py:668-698) or an
+    AGCCT_CONNECTOR in its frame, rotated back to global (cct.py:962-994)."""
+
+    def __init__(self, kl: numpy.ndarray, p0: numpy.ndarray, current: float, frame: Frame = None):
+        self.kl, self.p0, self.current, self.frame = kl, p0, current, frame
+
+    def field_at(self, point: V3) -> V3:
+        if approx_equal(self.current, 0, err=1e-6):
+            return (0.0, 0.0, 0.0)
+        if self.frame is None:
+            return segments_field_local(self.kl, self.p0, point)
+        return self.frame.vector_to_global(segments_field_local(self.kl, self.p0, self.frame.point_to_local(point)))
+
+
 class BeamlineOracle:
     """Magnet list with Beamline.magnetic_field_at (beamline.py:46-53)."""
 

@@ -54,8 +54,15 @@ def test_layer_records_checked_on_host(lib):
     import numpy as np
     from cctpy_gb300 import engine, workloads as W
     _, dipole = W.build_single_dipole()
-    rec = np.ascontiguousarray(np.stack([engine.layer_record(dipole)] * 2))
+    rec = np.ascontiguousarray(np.stack([engine.layer_record(dipole, 0), engine.layer_record(dipole, 46080)]))
     assert lib.cct_layer_segments(rec.ctypes.data_as(ctypes.c_void_p), 2) == 2 * 46080
+    gap = rec.copy()
+    gap[1, 30] = 50000                 # room for other current elements between the layers
+    assert lib.cct_layer_segments(gap.ctypes.data_as(ctypes.c_void_p), 2) == 50000 + 46080
+    bad = rec.copy()
+    bad[1, 30] = 46079                  # overlapping layers
+    assert lib.cct_layer_segments(bad.ctypes.data_as(ctypes.c_void_p), 2) == -1
+    assert "overlap" in _lib.last_error()
     bad = rec.copy()
     bad[1, 21] = 9                      # more tilt angles than a record holds
     assert lib.cct_layer_segments(bad.ctypes.data_as(ctypes.c_void_p), 2) == -1
