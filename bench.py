@@ -165,6 +165,26 @@ def measure_tracking(args, dev, rank):
         return best
 
     out = {}
+    # C0: the reference's CPU-runnable case, whole track (32 protons, 374 steps of 1 mm)
+    _, dip = W.build_single_dipole()
+    dsd = engine.design_of(dip)
+    dsd.packed()
+    p32 = W.single_dipole_particles(32, seed=0)
+    L0 = W.single_dipole_track_length()
+    n0 = int(np.ceil(L0 / 0.001))
+    c0 = {}
+    for prec in ("f32c", "f64"):
+        engine.track(dsd, p32, 0.002, 0.001, prec)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        engine.track(dsd, p32, L0, 0.001, prec)
+        torch.cuda.synchronize()
+        t = time.perf_counter() - t0
+        c0[prec] = {"seconds": t, "steps": n0, "us_per_stage": t / (4 * n0) * 1e6,
+                    "gpairs_per_s": 32 * n0 * 4 * dsd.n_segments / t / 1e9}
+    out["single_dipole"] = dict(
+        workload=f"single CCT dipole, {dsd.n_segments} segments; 32 protons 250 MeV through the whole "
+                 f"{L0:.4f} m arc at 1 mm ({n0} RK4 steps), one call (latency-bound: 1 particle block)", **c0)
     bl = W.build_gantry_section()
     ds = engine.design_of(bl)
     ds.packed()

@@ -240,7 +240,7 @@ __global__ void __launch_bounds__(kTrackBlock, kTrackMinBlocks) adjoint_kernel(A
         for (int stage = 3; stage >= 0; --stage, ++phase) {
             const PointSrc src{rec_at(P, step, stage, 0), kRec, A.adj + AD_A, kAdjD};
             if (P.precision == 0) {
-                for (int64_t u = next_unit(P, sm, phase); u < n_units; u = next_unit(P, sm, phase))
+                for (int64_t u = first_unit(); u < n_units; u = next_unit(P, sm, phase))
                     unit_grad_f64(A, u, step, stage, sm);
             } else if (P.ppt == 2) {
                 units_f32c<2, true>(P, src, sm, kt, phase, n_units);

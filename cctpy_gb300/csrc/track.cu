@@ -66,7 +66,7 @@ __global__ void __launch_bounds__(kTrackBlock, kTrackMinBlocks) track_kernel(Tra
     for (int step = P.step_begin; step < step_end; ++step) {
         for (int stage = 0; stage < 4; ++stage, ++phase) {
             if (P.precision == 0) {
-                for (int64_t u = next_unit(P, sm, phase); u < n_units; u = next_unit(P, sm, phase))
+                for (int64_t u = first_unit(); u < n_units; u = next_unit(P, sm, phase))
                     unit_field_f64(P, u, sm);
             } else if (P.ppt == 2) {
                 units_f32c<2, false>(P, stage_points(P), sm, kt, phase, n_units);

@@ -123,14 +123,16 @@ static __device__ bool grid_barrier(const TrackParams &P, TrackSmem &sm) {
     return sm.verdict != 0;
 }
 
-// Dynamic unit schedule.  Phase k of a launch hands out units from counter CW_NEXT0 + (k & 1);
-// the other counter is cleared during the phase's particle step (reset_next_unit, after the
-// grid barrier that ends the unit phase), so it is zero again when phase k + 1 starts.
-// Every unit writes its partial sums to its own slots, so which CTA takes which unit does
-// not change any result.
+// Unit schedule.  In every phase CTA b first takes unit b; further units come from counter
+// CW_NEXT0 + (k & 1) of phase k, offset by the grid size (so a phase with no more units than
+// CTAs costs no atomic at all).  The other counter is cleared during the phase's particle
+// step (reset_next_unit, after the grid barrier that ends the unit phase), so it is zero
+// again when phase k + 1 starts.  Every unit writes its partial sums to its own slots, so
+// which CTA takes which unit does not change any result.
+static __device__ __forceinline__ int64_t first_unit() { return (int64_t)blockIdx.x; }
 static __device__ __forceinline__ int64_t next_unit(const TrackParams &P, TrackSmem &sm, int phase) {
     __syncthreads();   // the previous value has been read by every thread
-    if (threadIdx.x == 0) sm.unit = (int64_t)atomicAdd(P.ctrl + CW_NEXT0 + (phase & 1), 1u);
+    if (threadIdx.x == 0) sm.unit = (int64_t)gridDim.x + (int64_t)atomicAdd(P.ctrl + CW_NEXT0 + (phase & 1), 1u);
     __syncthreads();
     return sm.unit;
 }
@@ -357,7 +359,7 @@ static __device__ int64_t unit_sum_f32c(const TrackParams &P, const PointSrc &sr
 template <int PPT, bool GRAD>
 static __device__ bool units_f32c(const TrackParams &P, const PointSrc &src, TrackSmem &sm, uint32_t &kt, int phase,
                                   int64_t n_units) {
-    int64_t u = next_unit(P, sm, phase);
+    int64_t u = first_unit();
     if (u < n_units) unit_prefetch(P, u, sm, kt);
     while (u < n_units) {
         u = unit_sum_f32c<PPT, GRAD>(P, src, u, sm, kt, phase, n_units);
@@ -367,8 +369,8 @@ static __device__ bool units_f32c(const TrackParams &P, const PointSrc &src, Tra
 }
 
 // Sum of the chunk partials of particle pi by the calling warp (all 32 lanes, converged):
-// lane l adds chunks l, l + 32, ... in turn, then a fixed shuffle tree; lane 0 gets the
-// total.  A fixed order (deterministic), and the chunk loads of one particle are spread
+// lane l adds chunks l, l + 32, ... into four accumulators in a fixed pattern, then a fixed
+// shuffle tree; lane 0 gets the total.  A fixed order (deterministic), and the chunk loads of one particle are spread
 // over the warp instead of one thread walking them in sequence.
 static __device__ __forceinline__ void warp_sum_partials(const TrackParams &P, int64_t pi, double out[3]) {
     const int lane = threadIdx.x & 31;
@@ -377,13 +379,32 @@ static __device__ __forceinline__ void warp_sum_partials(const TrackParams &P, i
     const int64_t b = j / P.G, slot = j % P.G;
     const int64_t cd = P.chunks[d];
     const int64_t u0 = P.unit_off[d] + b * cd;
-    double x = 0.0, y = 0.0, z = 0.0;
-    for (int64_t c = lane; c < cd; c += 32) {
-        const double *p = P.partial + ((u0 + c) * P.G + slot) * 3;
-        x += p[0];
-        y += p[1];
-        z += p[2];
+    // four independent accumulators, so that a lane has up to 12 loads in flight
+    double a[4][3] = {{0.0, 0.0, 0.0}, {0.0, 0.0, 0.0}, {0.0, 0.0, 0.0}, {0.0, 0.0, 0.0}};
+    int64_t c = lane;
+    for (; c + 96 < cd; c += 128) {
+        double v[4][3];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const double *p = P.partial + ((u0 + c + 32 * k) * P.G + slot) * 3;
+            v[k][0] = p[0];
+            v[k][1] = p[1];
+            v[k][2] = p[2];
+        }
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+#pragma unroll
+            for (int q = 0; q < 3; ++q) a[k][q] += v[k][q];
     }
+    for (; c < cd; c += 32) {
+        const double *p = P.partial + ((u0 + c) * P.G + slot) * 3;
+        a[0][0] += p[0];
+        a[0][1] += p[1];
+        a[0][2] += p[2];
+    }
+    double x = (a[0][0] + a[1][0]) + (a[2][0] + a[3][0]);
+    double y = (a[0][1] + a[1][1]) + (a[2][1] + a[3][1]);
+    double z = (a[0][2] + a[1][2]) + (a[2][2] + a[3][2]);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         x += __shfl_down_sync(0xffffffffu, x, o);
