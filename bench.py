@@ -295,15 +295,15 @@ def measure_design_grads(args, rank):
     n_seg = ds.n_segments
     out = {"workload": f"16 second-section designs ({n_seg} segments total), 1024 protons each, 13 parameters "
                        "(8 tilts, 4 layer currents, winding radius), J = <x^2>+<y^2> at the exit; "
-                       "checkpoints every 16 steps",
+                       "stage records of the whole slice kept in HBM (one checkpoint segment, no recompute)",
            "design_set_seconds": t_setup}
     for prec, steps in (("f32c", args.adjoint_steps), ("f64", max(1, args.adjoint_steps // 16))):
         L = steps * 0.001
         frames = np.tile(exit_frame(designs[0].beamline.trajectory, L, 215.0), (16, 1))
-        segment_gradient(ds, ps, 0.002, 0.001, frames, 16, prec)          # warm-up
+        segment_gradient(ds, ps, 0.002, 0.001, frames, None, prec)        # warm-up
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        J, seg, _ = segment_gradient(ds, ps, L, 0.001, frames, 16, prec, on_device=True)
+        J, seg, _ = segment_gradient(ds, ps, L, 0.001, frames, None, prec, on_device=True)
         torch.cuda.synchronize()
         t_gpu = time.perf_counter() - t0
         t0 = time.perf_counter()

@@ -53,11 +53,25 @@ def objective_host(final: np.ndarray, frame: np.ndarray) -> float:
     return float(np.mean(x * x + y * y))
 
 
+def auto_checkpoint(n_records: int, max_steps: int) -> int:
+    """Checkpoint interval (RK4 steps) for `n_records` tracked particles: the whole track in
+    one segment when its stage records (4 x 96 bytes per particle and step) fit in a quarter
+    of the free device memory (at most 64 GiB) -- the forward then records as it goes and
+    nothing is recomputed --, else as many steps per segment as that budget holds."""
+    free, _ = torch.cuda.mem_get_info()
+    budget = min(free // 4, 64 << 30)
+    per_step = 4 * 96 * int(n_records)
+    if per_step * max_steps <= budget:
+        return int(max_steps)
+    return int(max(16, budget // per_step))
+
+
 def segment_gradient(ds: engine.DesignSet, particles, distance: float, footstep: float, frames: np.ndarray,
-                     checkpoint: int = 64, precision: str = "f64", on_device: bool = False):
+                     checkpoint: int = None, precision: str = "f64", on_device: bool = False):
     """(J (D,), dJ/d(kl, p0) (N_seg, 6), final records (D, n, 10)) for the designs of `ds`;
-    precision "f64" or "f32c" (forward and adjoint sweeps).  on_device=True returns the
-    segment gradient as a CUDA tensor (for DesignSet.param_grad)."""
+    precision "f64" or "f32c" (forward and adjoint sweeps); checkpoint: RK4 steps per
+    checkpoint segment (None: auto_checkpoint).  on_device=True returns the segment gradient
+    as a CUDA tensor (for DesignSet.param_grad)."""
     lib = _lib.load()
     dev = ds.kls.device
     p = torch.as_tensor(np.asarray(particles, dtype=np.float64), device=dev)
@@ -72,6 +86,8 @@ def segment_gradient(ds: engine.DesignSet, particles, distance: float, footstep:
     fr = torch.as_tensor(np.asarray(frames, dtype=np.float64).reshape(ds.n_designs, 9), device=dev).contiguous()
     J = torch.empty(ds.n_designs, dtype=torch.float64, device=dev)
     grad = torch.empty((max(ds.n_segments, 1), 6), dtype=torch.float64, device=dev)
+    if checkpoint is None:
+        checkpoint = auto_checkpoint(ds.n_designs * n_p, max_steps)
     nbytes = lib.cct_adjoint_scratch_bytes(ds.n_designs, n_p, max_steps, checkpoint)
     _lib.check(0 if nbytes >= 0 else _lib.CCT_ERR_ARG, "cct_adjoint_scratch_bytes")
     prec = {"f64": 0, "f32c": 1}.get(precision)
@@ -214,7 +230,7 @@ def layer_grads_from_rows(magnets: Sequence, rows: np.ndarray) -> List[Dict[str,
 
 
 def design_gradients(designs: Sequence[GantryDesign], particles: np.ndarray, distance: float, footstep: float,
-                     kinetic_MeV: float, checkpoint: int = 64, precision: str = "f64",
+                     kinetic_MeV: float, checkpoint: int = None, precision: str = "f64",
                      jacobian: str = "device") -> Tuple[np.ndarray, np.ndarray]:
     """J (D,) and dJ/dtheta (D, 13) of every design, all tracked in one adjoint run.  The
     designs share the design orbit: particles start at s = 0 and the objective is read in

@@ -570,7 +570,8 @@ static int launch_adjoint(const double *kls, const double *p0s, const int64_t *s
     double *record = reinterpret_cast<double *>(sc + AL.record_off);
     const size_t state_bytes = 8 * (size_t)kStateD * tot;
 
-    // 2. forward in checkpoint segments
+    // 2. forward in checkpoint segments; the last one records its stages right away, so the
+    //    reverse sweep starts without recomputing it (with one segment: no recompute at all)
     P.init_from_records = 0;
     for (int c = 0; c < n_ckpt; ++c) {
         CCT_TRY_CUDA(cudaMemcpyAsync(ckpt + (int64_t)c * kStateD * tot, P.state, state_bytes, cudaMemcpyDeviceToDevice,
@@ -578,8 +579,10 @@ static int launch_adjoint(const double *kls, const double *p0s, const int64_t *s
         P.step_begin = c * K;
         P.step_end = std::min(steps, (c + 1) * K);
         P.write_back = c == n_ckpt - 1;
+        P.record = c == n_ckpt - 1 ? record : nullptr;
         CCT_TRY_CUDA(launch_track_kernel(P, grid, st));
     }
+    P.record = nullptr;
 
     // 3. objective and the adjoint of the final state
     AdjParams A;
@@ -595,13 +598,15 @@ static int launch_adjoint(const double *kls, const double *p0s, const int64_t *s
     int64_t max_seg = 0;
     for (int d = 0; d < n_designs; ++d) max_seg = std::max(max_seg, hoff[d + 1] - hoff[d]);
     for (int c = n_ckpt - 1; c >= 0; --c) {
-        CCT_TRY_CUDA(cudaMemcpyAsync(P.state, ckpt + (int64_t)c * kStateD * tot, state_bytes, cudaMemcpyDeviceToDevice,
-                                     st));
         P.step_begin = c * K;
         P.step_end = std::min(steps, (c + 1) * K);
         P.write_back = 0;
         P.record = record;
-        CCT_TRY_CUDA(launch_track_kernel(P, grid, st));
+        if (c < n_ckpt - 1) {   // recompute this segment from its checkpoint, recording its stages
+            CCT_TRY_CUDA(cudaMemcpyAsync(P.state, ckpt + (int64_t)c * kStateD * tot, state_bytes,
+                                         cudaMemcpyDeviceToDevice, st));
+            CCT_TRY_CUDA(launch_track_kernel(P, grid, st));
+        }
         A.T = P;
         A.T.barrier_blocks = (unsigned)(agrid + g_test_phantom_blocks);
         A.step_begin = P.step_begin;
