@@ -332,12 +332,30 @@ __global__ void __launch_bounds__(kSegBlock) seg_adjoint_kernel(TrackParams P, i
     }
 }
 
-// FP32c segment gradient: one warp per packed tile, four segments per lane (two packed
-// pairs); the design's recorded (p, a) pairs are staged in shared memory in the tile's local
-// double-float frame, 128 at a time; per-chunk FP32 sums are Kahan-compensated per segment.
+// FP32c segment gradient.  seg_prep_kernel converts every recorded stage point once: its
+// position as a double-float pair (hi, lo) and its weight a in FP32, three float4 per point
+// {hx, hy, hz, ax}, {lx, ly, lz, ay}, {az, 0, 0, 0}.  seg_adjoint_f32c_kernel then runs one
+// 64-thread CTA per packed tile, two segments per thread (one packed pair); the design's
+// points are staged in shared memory 128 at a time in the tile's local frame (point minus
+// tile origin in double-float FP32, no FP64 work per tile), and the per-chunk FP32 sums are
+// Kahan-compensated per segment.
 constexpr int kSegPts = 128;
+constexpr int kSegThreads = 64;
 
-__global__ void __launch_bounds__(32) seg_adjoint_f32c_kernel(TrackParams P, int n_steps, double *grad) {
+__global__ void seg_prep_kernel(const double *__restrict__ record, int64_t n_rec, float4 *__restrict__ out) {
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n_rec; e += (int64_t)gridDim.x * blockDim.x) {
+        const double *r = record + e * kRec;
+        float h[3], l[3];
+        for (int c = 0; c < 3; ++c) split_df(r[c], h[c], l[c]);
+        out[3 * e] = make_float4(h[0], h[1], h[2], (float)r[9]);
+        out[3 * e + 1] = make_float4(l[0], l[1], l[2], (float)r[10]);
+        out[3 * e + 2] = make_float4((float)r[11], 0.0f, 0.0f, 0.0f);
+    }
+}
+
+__global__ void __launch_bounds__(kSegThreads, 8) seg_adjoint_f32c_kernel(TrackParams P, int n_steps,
+                                                                          const float4 *__restrict__ pts_df,
+                                                                          double *grad) {
     __shared__ __align__(16) f2 pts[kSegPts][9];   // (q,q) x3, (a,a) x3, (-a,-a) x3
     const int64_t t = blockIdx.x;
     int lo = 0, hi = P.n_designs - 1;               // design of tile t: last d with tile_off[d] <= t
@@ -348,17 +366,18 @@ __global__ void __launch_bounds__(32) seg_adjoint_f32c_kernel(TrackParams P, int
     const int d = lo;
     const unsigned char *tile = P.tiles + t * (int64_t)kTileBytes;
     const TileHeader *h = reinterpret_cast<const TileHeader *>(tile);
-    const ulonglong2 *v = reinterpret_cast<const ulonglong2 *>(tile + kTileHeaderBytes);
-    constexpr int Q = kTile / 4;
-    const int lane = threadIdx.x;
+    const f2 *v = reinterpret_cast<const f2 *>(tile + kTileHeaderBytes);
+    constexpr int Q2 = kTile / 2;                   // packed pairs per component array
+    const int tid = threadIdx.x;
     const int cnt = h->count;
     const int64_t s0 = P.seg_off[d] + (t - P.tile_off[d]) * kTile;
-    ulonglong2 K[9];
+    f2 K[9];
 #pragma unroll
-    for (int c = 0; c < 9; ++c) K[c] = v[c * Q + lane];
-    float S[4][6], C[4][6];
+    for (int c = 0; c < 9; ++c) K[c] = v[c * Q2 + tid];
+    const f2 kx = K[0], ky = K[1], kz = K[2], nx = K[3], ny = K[4], nz = K[5], px = K[6], py = K[7], pz = K[8];
+    float S[2][6], C[2][6];
 #pragma unroll
-    for (int m = 0; m < 4; ++m)
+    for (int m = 0; m < 2; ++m)
 #pragma unroll
         for (int c = 0; c < 6; ++c) S[m][c] = C[m][c] = 0.0f;
     const f2 m3 = f2_pack(-3.0f, -3.0f);
@@ -366,17 +385,18 @@ __global__ void __launch_bounds__(32) seg_adjoint_f32c_kernel(TrackParams P, int
     const int64_t n_pts = (int64_t)n_steps * 4 * P.n_p;
     for (int64_t base = 0; base < n_pts; base += kSegPts) {
         __syncthreads();
-        for (int k = lane; k < kSegPts; k += 32) {
+        for (int k = tid; k < kSegPts; k += kSegThreads) {
             const int64_t e = base + k;
             float q[3] = {0.f, 0.f, 0.f}, a[3] = {0.f, 0.f, 0.f};
             if (e < n_pts) {
-                const double *r = P.record + ((e / P.n_p) * total + (int64_t)d * P.n_p + e % P.n_p) * kRec;
-                for (int c = 0; c < 3; ++c) {
-                    float ph, pl;
-                    split_df(r[c], ph, pl);
-                    q[c] = __fadd_rn(__fsub_rn(ph, h->o_hi[c]), __fsub_rn(pl, h->o_lo[c]));
-                    a[c] = (float)r[9 + c];
-                }
+                const float4 *r = pts_df + 3 * ((e / P.n_p) * total + (int64_t)d * P.n_p + e % P.n_p);
+                const float4 u = r[0], w = r[1], z = r[2];
+                q[0] = __fadd_rn(__fsub_rn(u.x, h->o_hi[0]), __fsub_rn(w.x, h->o_lo[0]));
+                q[1] = __fadd_rn(__fsub_rn(u.y, h->o_hi[1]), __fsub_rn(w.y, h->o_lo[1]));
+                q[2] = __fadd_rn(__fsub_rn(u.z, h->o_hi[2]), __fsub_rn(w.z, h->o_lo[2]));
+                a[0] = u.w;
+                a[1] = w.w;
+                a[2] = z.x;
             }
             for (int c = 0; c < 3; ++c) {
                 pts[k][c] = f2_pack(q[c], q[c]);
@@ -385,64 +405,52 @@ __global__ void __launch_bounds__(32) seg_adjoint_f32c_kernel(TrackParams P, int
             }
         }
         __syncthreads();
-        f2 KL[2][3], PZ[2][3];
-#pragma unroll
-        for (int m = 0; m < 2; ++m)
-#pragma unroll
-            for (int c = 0; c < 3; ++c) KL[m][c] = PZ[m][c] = 0ull;
+        f2 KL[3] = {0ull, 0ull, 0ull}, PZ[3] = {0ull, 0ull, 0ull};
         const int np = (int)min((int64_t)kSegPts, n_pts - base);
-#pragma unroll 1
+#pragma unroll 2
         for (int i = 0; i < np; ++i) {
             const f2 Ax = pts[i][3], Ay = pts[i][4], Az = pts[i][5];
-            if ((Ax | Ay | Az) == 0ull) continue;              // inactive stage: uniform over the warp
+            if ((Ax | Ay | Az) == 0ull) continue;              // inactive stage: uniform over the CTA
             const f2 Qx = pts[i][0], Qy = pts[i][1], Qz = pts[i][2];
             const f2 NAx = pts[i][6], NAy = pts[i][7], NAz = pts[i][8];
-#pragma unroll
-            for (int m = 0; m < 2; ++m) {
-                const f2 kx = m ? K[0].y : K[0].x, ky = m ? K[1].y : K[1].x, kz = m ? K[2].y : K[2].x;
-                const f2 nx = m ? K[3].y : K[3].x, ny = m ? K[4].y : K[4].x, nz = m ? K[5].y : K[5].x;
-                const f2 px = m ? K[6].y : K[6].x, py = m ? K[7].y : K[7].x, pz = m ? K[8].y : K[8].x;
-                const f2 rx = f2_sub(Qx, px), ry = f2_sub(Qy, py), rz = f2_sub(Qz, pz);
-                const f2 r2 = f2_fma(rx, rx, f2_fma(ry, ry, f2_mul(rz, rz)));
-                float l0, l1;
-                f2_unpack(r2, l0, l1);
-                const f2 inv = f2_pack(rsqrt_mufu(l0), rsqrt_mufu(l1));
-                const f2 inv2 = f2_mul(inv, inv);
-                const f2 inv3 = f2_mul(inv2, inv);
-                const f2 m3inv5 = f2_mul(f2_mul(inv3, inv2), m3);
-                // r x a
-                const f2 rax = f2_fma(ry, Az, f2_mul(rz, NAy));
-                const f2 ray = f2_fma(rz, Ax, f2_mul(rx, NAz));
-                const f2 raz = f2_fma(rx, Ay, f2_mul(ry, NAx));
-                KL[m][0] = f2_fma(rax, inv3, KL[m][0]);
-                KL[m][1] = f2_fma(ray, inv3, KL[m][1]);
-                KL[m][2] = f2_fma(raz, inv3, KL[m][2]);
-                // c = a x kl; grad_p (a . B_i) = c inv3 - 3 (c.r) inv5 r
-                const f2 cx = f2_fma(Ay, kz, f2_mul(Az, ny));
-                const f2 cy = f2_fma(Az, kx, f2_mul(Ax, nz));
-                const f2 cz = f2_fma(Ax, ky, f2_mul(Ay, nx));
-                const f2 nq = f2_mul(f2_fma(cx, rx, f2_fma(cy, ry, f2_mul(cz, rz))), m3inv5);
-                PZ[m][0] = f2_fma(nq, rx, f2_fma(cx, inv3, PZ[m][0]));
-                PZ[m][1] = f2_fma(nq, ry, f2_fma(cy, inv3, PZ[m][1]));
-                PZ[m][2] = f2_fma(nq, rz, f2_fma(cz, inv3, PZ[m][2]));
-            }
+            const f2 rx = f2_sub(Qx, px), ry = f2_sub(Qy, py), rz = f2_sub(Qz, pz);
+            const f2 r2 = f2_fma(rx, rx, f2_fma(ry, ry, f2_mul(rz, rz)));
+            float l0, l1;
+            f2_unpack(r2, l0, l1);
+            const f2 inv = f2_pack(rsqrt_mufu(l0), rsqrt_mufu(l1));
+            const f2 inv2 = f2_mul(inv, inv);
+            const f2 inv3 = f2_mul(inv2, inv);
+            const f2 m3inv5 = f2_mul(f2_mul(inv3, inv2), m3);
+            // r x a
+            const f2 rax = f2_fma(ry, Az, f2_mul(rz, NAy));
+            const f2 ray = f2_fma(rz, Ax, f2_mul(rx, NAz));
+            const f2 raz = f2_fma(rx, Ay, f2_mul(ry, NAx));
+            KL[0] = f2_fma(rax, inv3, KL[0]);
+            KL[1] = f2_fma(ray, inv3, KL[1]);
+            KL[2] = f2_fma(raz, inv3, KL[2]);
+            // c = a x kl; grad_p (a . B_i) = c inv3 - 3 (c.r) inv5 r
+            const f2 cx = f2_fma(Ay, kz, f2_mul(Az, ny));
+            const f2 cy = f2_fma(Az, kx, f2_mul(Ax, nz));
+            const f2 cz = f2_fma(Ax, ky, f2_mul(Ay, nx));
+            const f2 nq = f2_mul(f2_fma(cx, rx, f2_fma(cy, ry, f2_mul(cz, rz))), m3inv5);
+            PZ[0] = f2_fma(nq, rx, f2_fma(cx, inv3, PZ[0]));
+            PZ[1] = f2_fma(nq, ry, f2_fma(cy, inv3, PZ[1]));
+            PZ[2] = f2_fma(nq, rz, f2_fma(cz, inv3, PZ[2]));
         }
 #pragma unroll
-        for (int m = 0; m < 2; ++m)
-#pragma unroll
-            for (int c = 0; c < 3; ++c) {
-                float e0, e1;
-                f2_unpack(KL[m][c], e0, e1);
-                kahan_add(S[2 * m][c], C[2 * m][c], e0);
-                kahan_add(S[2 * m + 1][c], C[2 * m + 1][c], e1);
-                f2_unpack(PZ[m][c], e0, e1);
-                kahan_add(S[2 * m][3 + c], C[2 * m][3 + c], e0);
-                kahan_add(S[2 * m + 1][3 + c], C[2 * m + 1][3 + c], e1);
-            }
+        for (int c = 0; c < 3; ++c) {
+            float e0, e1;
+            f2_unpack(KL[c], e0, e1);
+            kahan_add(S[0][c], C[0][c], e0);
+            kahan_add(S[1][c], C[1][c], e1);
+            f2_unpack(PZ[c], e0, e1);
+            kahan_add(S[0][3 + c], C[0][3 + c], e0);
+            kahan_add(S[1][3 + c], C[1][3 + c], e1);
+        }
     }
 #pragma unroll
-    for (int m = 0; m < 4; ++m) {
-        const int j = 4 * lane + m;
+    for (int m = 0; m < 2; ++m) {
+        const int j = 2 * tid + m;
         if (j >= cnt) continue;
         double *g = grad + 6 * (s0 + j);
         for (int c = 0; c < 3; ++c) g[c] += (double)S[m][c] - (double)C[m][c];
@@ -452,7 +460,7 @@ __global__ void __launch_bounds__(32) seg_adjoint_f32c_kernel(TrackParams P, int
 
 // ---------------------------------------------------------------- host side
 struct AdjLayout {
-    int64_t track_total, ckpt_off, record_off, adj_off, total;
+    int64_t track_total, ckpt_off, record_off, adj_off, pts_off, total;
 };
 
 static AdjLayout adj_layout(const TrackScratchLayout &L, int n_designs, int64_t n_p, int n_ckpt, int K) {
@@ -463,7 +471,8 @@ static AdjLayout adj_layout(const TrackScratchLayout &L, int n_designs, int64_t 
     A.ckpt_off = up(L.total);
     A.record_off = A.ckpt_off + up(8 * kStateD * tot * (int64_t)n_ckpt);
     A.adj_off = A.record_off + up(8 * (int64_t)kRec * 4 * K * tot);
-    A.total = A.adj_off + up(8 * kAdjD * tot);
+    A.pts_off = A.adj_off + up(8 * kAdjD * tot);                   // FP32c: converted stage points
+    A.total = A.pts_off + up(48 * (int64_t)4 * K * tot);
     return A;
 }
 
@@ -615,7 +624,13 @@ static int launch_adjoint(const double *kls, const double *p0s, const int64_t *s
         CCT_TRY_CUDA(cudaLaunchCooperativeKernel((const void *)adjoint_kernel, dim3(agrid), dim3(kTrackBlock), args,
                                                  0, st));
         if (precision == 1 && tiles_total > 0) {
-            seg_adjoint_f32c_kernel<<<(unsigned)tiles_total, 32, 0, st>>>(P, P.step_end - P.step_begin, seg_grad);
+            const int64_t n_rec = (int64_t)(P.step_end - P.step_begin) * 4 * tot;
+            float4 *pts_df = reinterpret_cast<float4 *>(sc + AL.pts_off);
+            const int64_t prep_blocks = std::min<int64_t>((n_rec + 255) / 256, 65536);
+            seg_prep_kernel<<<(unsigned)std::max<int64_t>(prep_blocks, 1), 256, 0, st>>>(record, n_rec, pts_df);
+            CCT_TRY_CUDA(cudaGetLastError());
+            seg_adjoint_f32c_kernel<<<(unsigned)tiles_total, kSegThreads, 0, st>>>(P, P.step_end - P.step_begin,
+                                                                                   pts_df, seg_grad);
             CCT_TRY_CUDA(cudaGetLastError());
         } else if (precision == 0 && max_seg > 0) {
             const dim3 sg((unsigned)((max_seg + kSegBlock - 1) / kSegBlock), (unsigned)n_designs);
