@@ -271,13 +271,15 @@ __global__ void __launch_bounds__(kF32Block, kF32Blocks) field_f32c_kernel(const
         }
     }
 
-    float ph[kF32Ppt][3], pl[kF32Ppt][3];
+    // each thread's points as double-float pairs in shared memory (only that thread reads them):
+    // spt[c][i][tid], c = hi x, y, z, lo x, y, z
+    __shared__ float spt[6][kF32Ppt][kF32Block];
 #pragma unroll
     for (int i = 0; i < kF32Ppt; ++i) {
         int64_t idx = base + tid + (int64_t)i * kF32Block;
         if (idx >= n) idx = n - 1;
 #pragma unroll
-        for (int c = 0; c < 3; ++c) split_df(pts[3 * idx + c], ph[i][c], pl[i][c]);
+        for (int c = 0; c < 3; ++c) split_df(pts[3 * idx + c], spt[c][i][tid], spt[3 + c][i][tid]);
     }
     F32cAcc<kF32Ppt> acc;
     acc.zero();
@@ -292,7 +294,7 @@ __global__ void __launch_bounds__(kF32Block, kF32Blocks) field_f32c_kernel(const
             failed = true;
             break;
         }
-        tile_f32c<kF32Ppt, kF32Unroll>(buf[s], ph, pl, acc);
+        tile_f32c_smem<kF32Ppt, kF32Unroll>(buf[s], &spt[0][0][tid], kF32Block, acc);
         if (cctdev::ring_release_last(&released[s], kWarps) && t + kStages < nt) {
             last_issued[s] = t + kStages;
             cctdev::fence_proxy_async();

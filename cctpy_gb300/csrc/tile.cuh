@@ -78,14 +78,10 @@ struct F32cAcc {
 // Accumulate segments [4*g0, 4*g1) of one tile (default: all 128) for PPT points given as
 // double-float (hi, lo) coordinates.  JU: unroll of the 4-segment loop (2 keeps more
 // independent pair terms in flight where registers allow).
-template <int PPT, int JU = 1>
-__device__ __forceinline__ void tile_f32c(const unsigned char *tile, const float (&ph)[PPT][3],
-                                          const float (&pl)[PPT][3], F32cAcc<PPT> &acc, int g0 = 0,
-                                          int g1 = kTile / 4) {
-    const TileHeader *h = reinterpret_cast<const TileHeader *>(tile);
-    const ulonglong2 *v = reinterpret_cast<const ulonglong2 *>(tile + kTileHeaderBytes);
-    constexpr int Q = kTile / 4;   // ulonglong2 (4 floats) per component array
-    f2 q[PPT][3];
+// The point offsets from the tile origin, q = (p_hi - o_hi) + (p_lo - o_lo) in FP32, packed.
+template <int PPT>
+__device__ __forceinline__ void tile_offsets(const TileHeader *h, const float (&ph)[PPT][3], const float (&pl)[PPT][3],
+                                             f2 (&q)[PPT][3]) {
 #pragma unroll
     for (int i = 0; i < PPT; ++i)
 #pragma unroll
@@ -93,6 +89,45 @@ __device__ __forceinline__ void tile_f32c(const unsigned char *tile, const float
             const float d = __fadd_rn(__fsub_rn(ph[i][c], h->o_hi[c]), __fsub_rn(pl[i][c], h->o_lo[c]));
             q[i][c] = f2_pack(d, d);
         }
+}
+
+template <int PPT, int JU>
+__device__ __forceinline__ void tile_pairs(const unsigned char *tile, const f2 (&q)[PPT][3], F32cAcc<PPT> &acc,
+                                           int g0, int g1);
+
+template <int PPT, int JU = 1>
+__device__ __forceinline__ void tile_f32c(const unsigned char *tile, const float (&ph)[PPT][3],
+                                          const float (&pl)[PPT][3], F32cAcc<PPT> &acc, int g0 = 0,
+                                          int g1 = kTile / 4) {
+    f2 q[PPT][3];
+    tile_offsets<PPT>(reinterpret_cast<const TileHeader *>(tile), ph, pl, q);
+    tile_pairs<PPT, JU>(tile, q, acc, g0, g1);
+}
+
+// The same with the point's double-float coordinates kept in shared memory: component c
+// (hi x, y, z, lo x, y, z) of point i at sp[(c * PPT + i) * stride], so that they hold no
+// registers during the segment loop.
+template <int PPT, int JU = 1>
+__device__ __forceinline__ void tile_f32c_smem(const unsigned char *tile, const float *sp, int stride,
+                                               F32cAcc<PPT> &acc) {
+    float ph[PPT][3], pl[PPT][3];
+#pragma unroll
+    for (int i = 0; i < PPT; ++i)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            ph[i][c] = sp[(c * PPT + i) * stride];
+            pl[i][c] = sp[((3 + c) * PPT + i) * stride];
+        }
+    f2 q[PPT][3];
+    tile_offsets<PPT>(reinterpret_cast<const TileHeader *>(tile), ph, pl, q);
+    tile_pairs<PPT, JU>(tile, q, acc, 0, kTile / 4);
+}
+
+template <int PPT, int JU>
+__device__ __forceinline__ void tile_pairs(const unsigned char *tile, const f2 (&q)[PPT][3], F32cAcc<PPT> &acc,
+                                           int g0, int g1) {
+    const ulonglong2 *v = reinterpret_cast<const ulonglong2 *>(tile + kTileHeaderBytes);
+    constexpr int Q = kTile / 4;   // ulonglong2 (4 floats) per component array
 #pragma unroll 1
     for (int sb = g0; sb < g1; sb += 16) {                       // sub-blocks of <= 64 segments
         const int se = min(sb + 16, g1);
