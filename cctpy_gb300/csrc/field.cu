@@ -294,7 +294,7 @@ __global__ void __launch_bounds__(kF32Block, kF32Blocks) field_f32c_kernel(const
             failed = true;
             break;
         }
-        tile_f32c_smem<kF32Ppt, kF32Unroll>(buf[s], &spt[0][0][tid], kF32Block, acc);
+        tile_f32c_smem<kF32Ppt, kF32Unroll>(buf[s], &spt[0][0][tid], kF32Ppt * kF32Block, kF32Block, acc);
         if (cctdev::ring_release_last(&released[s], kWarps) && t + kStages < nt) {
             last_issued[s] = t + kStages;
             cctdev::fence_proxy_async();

@@ -105,22 +105,22 @@ __device__ __forceinline__ void tile_f32c(const unsigned char *tile, const float
 }
 
 // The same with the point's double-float coordinates kept in shared memory: component c
-// (hi x, y, z, lo x, y, z) of point i at sp[(c * PPT + i) * stride], so that they hold no
-// registers during the segment loop.
+// (hi x, y, z, lo x, y, z) of point i at sp[c * c_stride + i * i_stride], so that they hold
+// no registers during the segment loop.
 template <int PPT, int JU = 1>
-__device__ __forceinline__ void tile_f32c_smem(const unsigned char *tile, const float *sp, int stride,
-                                               F32cAcc<PPT> &acc) {
+__device__ __forceinline__ void tile_f32c_smem(const unsigned char *tile, const float *sp, int c_stride, int i_stride,
+                                               F32cAcc<PPT> &acc, int g0 = 0, int g1 = kTile / 4) {
     float ph[PPT][3], pl[PPT][3];
 #pragma unroll
     for (int i = 0; i < PPT; ++i)
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
-            ph[i][c] = sp[(c * PPT + i) * stride];
-            pl[i][c] = sp[((3 + c) * PPT + i) * stride];
+            ph[i][c] = sp[c * c_stride + i * i_stride];
+            pl[i][c] = sp[(3 + c) * c_stride + i * i_stride];
         }
     f2 q[PPT][3];
     tile_offsets<PPT>(reinterpret_cast<const TileHeader *>(tile), ph, pl, q);
-    tile_pairs<PPT, JU>(tile, q, acc, 0, kTile / 4);
+    tile_pairs<PPT, JU>(tile, q, acc, g0, g1);
 }
 
 template <int PPT, int JU>
