@@ -200,6 +200,19 @@ def measure_tracking(args, dev, rank):
         "f32c": {"steps": s32, "seconds": t32, "particle_steps_per_s": r32, "gpairs_per_s": r32 * 4 * n_seg / 1e9},
         "f64": {"steps": s64, "seconds": t64, "particle_steps_per_s": r64, "gpairs_per_s": r64 * 4 * n_seg / 1e9},
         "speedup_f32c_vs_f64": r32 / r64}
+
+    def tuned(ds_, ps_, steps, n_p):
+        """The same FP32c slice after cct_autotune picked the work split for this problem."""
+        best = engine.autotune(ds_, ps_, 0.001, "f32c", steps=2)
+        try:
+            t = timed(ds_, ps_, steps, "f32c")
+        finally:
+            engine.set_units_per_cta(0)
+        r = ds_.n_designs * n_p * steps / t
+        return {"units_per_cta": best, "seconds": t, "particle_steps_per_s": r,
+                "gpairs_per_s": n_p * steps * 4 * ds_.n_segments / t / 1e9}
+
+    out["gantry_section"]["f32c_autotuned"] = tuned(ds, ps, s32, 4096)
     if not args.no_population:
         bls = [HUST_SC_GANTRY(**kw).create_second_bending_part_beamline() for kw in W.design_population(64, seed=3)]
         dsp = engine.design_set_of(bls)
@@ -212,7 +225,8 @@ def measure_tracking(args, dev, rank):
             "workload": f"64 designs ({min(segs)}..{max(segs)} segments, {dsp.n_segments} total), 512 protons each, "
                         "one launch",
             "f32c": {"steps": s32 // 2, "seconds": tp, "particle_steps_per_s": rp,
-                     "gpairs_per_s": 512 * (s32 // 2) * 4 * dsp.n_segments / tp / 1e9}}
+                     "gpairs_per_s": 512 * (s32 // 2) * 4 * dsp.n_segments / tp / 1e9},
+            "f32c_autotuned": tuned(dsp, pp, s32 // 2, 512)}
     if not args.no_adjoint:
         out["design_gradients"] = measure_design_grads(args, rank)
     if not args.no_generation:
