@@ -371,10 +371,8 @@ __global__ void __launch_bounds__(kSegThreads, 8) seg_adjoint_f32c_kernel(TrackP
     const int tid = threadIdx.x;
     const int cnt = h->count;
     const int64_t s0 = P.seg_off[d] + (t - P.tile_off[d]) * kTile;
-    f2 K[9];
-#pragma unroll
-    for (int c = 0; c < 9; ++c) K[c] = v[c * Q2 + tid];
-    const f2 kx = K[0], ky = K[1], kz = K[2], nx = K[3], ny = K[4], nz = K[5], px = K[6], py = K[7], pz = K[8];
+    const f2 kx = v[0 * Q2 + tid], ky = v[1 * Q2 + tid], kz = v[2 * Q2 + tid];
+    const f2 px = v[6 * Q2 + tid], py = v[7 * Q2 + tid], pz = v[8 * Q2 + tid];
     float S[2][6], C[2][6];
 #pragma unroll
     for (int m = 0; m < 2; ++m)
@@ -429,9 +427,9 @@ __global__ void __launch_bounds__(kSegThreads, 8) seg_adjoint_f32c_kernel(TrackP
             KL[1] = f2_fma(ray, inv3, KL[1]);
             KL[2] = f2_fma(raz, inv3, KL[2]);
             // c = a x kl; grad_p (a . B_i) = c inv3 - 3 (c.r) inv5 r
-            const f2 cx = f2_fma(Ay, kz, f2_mul(Az, ny));
-            const f2 cy = f2_fma(Az, kx, f2_mul(Ax, nz));
-            const f2 cz = f2_fma(Ax, ky, f2_mul(Ay, nx));
+            const f2 cx = f2_fma(Ay, kz, f2_mul(NAz, ky));
+            const f2 cy = f2_fma(Az, kx, f2_mul(NAx, kz));
+            const f2 cz = f2_fma(Ax, ky, f2_mul(NAy, kx));
             const f2 nq = f2_mul(f2_fma(cx, rx, f2_fma(cy, ry, f2_mul(cz, rz))), m3inv5);
             PZ[0] = f2_fma(nq, rx, f2_fma(cx, inv3, PZ[0]));
             PZ[1] = f2_fma(nq, ry, f2_fma(cy, inv3, PZ[1]));

@@ -9,9 +9,11 @@
 //  * field_f32c_kernel  FP32 arithmetic on per-tile local offsets: each tile of 128 segments
 //                       carries a double-float origin, point-minus-origin is taken in
 //                       double-float, the pair terms run as packed FP32x2 (two segments
-//                       per instruction; rsqrt on the MUFU pipe), summed in FP32 over
-//                       sub-blocks of 64 segments into a Kahan-compensated (S, C) pair
-//                       resolved in FP64 at the end (tile.cuh).  Tiles are streamed into
+//                       per instruction; rsqrt on the MUFU pipe) in the moment form
+//                       (sums of kl |r|^-3 and (kl x p0) |r|^-3 per 64-segment
+//                       sub-block, crossed with the point once per sub-block), summed into
+//                       a Kahan-compensated (S, C) pair resolved in FP64 at the end
+//                       (tile.cuh).  Tiles are streamed into
 //                       shared memory by the TMA bulk-copy engine through a 4-deep
 //                       mbarrier ring.
 #include <cstdarg>
@@ -112,7 +114,9 @@ int launch_field_f64(const double *kls, const double *p0s, int64_t n_seg, const 
 // ===================================================================== FP32c pack
 // Packs FP64 segments into FP32c tiles (layout in tile.cuh).  The tile origin is the
 // centroid of the tile's midpoints rounded to a double-float (hi, lo) pair; offsets are
-// taken from that represented origin, so point - origin needs no FP64 in the kernels.
+// taken from that represented origin, so point - origin needs no FP64 in the kernels.  Each
+// 64-segment sub-block gets its own FP32 origin (centroid of its offsets), about which the
+// moments kl x (p0 - origin - sub-block origin) are formed in FP64 and rounded once.
 __global__ void __launch_bounds__(kTile) pack_f32c_kernel(const double *__restrict__ kls,
                                                           const double *__restrict__ p0s,
                                                           unsigned char *__restrict__ packed) {
@@ -158,6 +162,26 @@ __global__ void __launch_bounds__(kTile) pack_f32c_kernel(const double *__restri
         split_df(cnt > 0 ? red[c][0] / cnt : 0.0, ohi[c], olo[c]);
         o[c] = (double)ohi[c] + (double)olo[c];
     }
+    // sub-block origins: FP32 centroid of the sub-block's offsets from the tile origin
+    double off[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) off[c] = p[c] - o[c];
+    __syncthreads();                              // everyone has read red[c][0]
+#pragma unroll
+    for (int c = 0; c < 3; ++c) red[c][i] = i < cnt ? off[c] : 0.0;
+    __syncthreads();
+    for (int w = kSub / 2; w > 0; w >>= 1) {      // fixed-order tree within each sub-block
+        if (i % kSub < w) {
+#pragma unroll
+            for (int c = 0; c < 3; ++c) red[c][i] += red[c][i + w];
+        }
+        __syncthreads();
+    }
+    const int sbk = i / kSub;
+    const int cnt_sb = min(max(cnt - sbk * kSub, 0), kSub);
+    float so[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) so[c] = cnt_sb > 0 ? (float)(red[c][sbk * kSub] / cnt_sb) : 0.0f;
 
     unsigned char *tile = tiles + t * (int64_t)kTileBytes;
     TileHeader *hdr = reinterpret_cast<TileHeader *>(tile);
@@ -170,14 +194,21 @@ __global__ void __launch_bounds__(kTile) pack_f32c_kernel(const double *__restri
         }
         hdr->count = cnt;
         hdr->pad = 0;
+        hdr->pad2[0] = hdr->pad2[1] = 0.0f;
+    }
+    if (i % kSub == 0) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) hdr->sub_o[sbk][c] = so[c];
     }
     if (i < cnt) {
+        // kl x (p0 - origin - sub-block origin), in FP64, rounded once
+        const double e[3] = {off[0] - (double)so[0], off[1] - (double)so[1], off[2] - (double)so[2]};
+        const double m[3] = {k[1] * e[2] - k[2] * e[1], k[2] * e[0] - k[0] * e[2], k[0] * e[1] - k[1] * e[0]};
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
-            const float kf = (float)k[c];
-            f[c * kTile + i] = kf;
-            f[(3 + c) * kTile + i] = -kf;
-            f[(6 + c) * kTile + i] = (float)(p[c] - o[c]);
+            f[c * kTile + i] = (float)k[c];
+            f[(3 + c) * kTile + i] = (float)m[c];
+            f[(6 + c) * kTile + i] = (float)off[c];
         }
     } else {   // padding: zero current element far away (contributes exactly 0)
 #pragma unroll

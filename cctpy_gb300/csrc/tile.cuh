@@ -1,15 +1,24 @@
 // One FP32-compensated tile of the packed segment form, shared by the field-map and
 // tracking kernels.
 //
-// Tile (kTileBytes = 4640 = 16 * 290):
+// Tile (kTileBytes = 4672 = 16 * 292):
 //   float o_hi[3], o_lo[3];  int count; int pad;      origin = o_hi + o_lo (double-float)
+//   float sub_o[2][3]; float pad2[2];                 origin of each 64-segment sub-block,
+//                                                     relative to the tile origin
 //   float kx[128], ky[128], kz[128];                   kl
-//   float nkx[128], nky[128], nkz[128];                -kl
+//   float mx[128], my[128], mz[128];                   kl x (p0 - origin - sub_o)
 //   float px[128], py[128], pz[128];                   p0 - origin
-// Arithmetic: packed FP32 pairs (PTX f32x2, two segments per instruction) for every
-// multiply/add of the pair term; rsqrt on the MUFU pipe; each half accumulates its
-// segments in FP32 over a sub-block of 64 segments, the sub-block sum is added to a
-// Kahan-compensated (S, C) pair, and S - C is taken in FP64 at the end.
+// Arithmetic ("moment form"): over a sub-block with origin o,
+//   sum_i kl_i x (q - p_i) |r_i|^-3 = A x (q - o) - M,  A = sum_i kl_i |r_i|^-3,
+//                                                        M = sum_i (kl_i x (p_i - o)) |r_i|^-3,
+// so a pair costs r = q - p_i, |r|^2, rsqrt, |r|^-3 and the six multiply-adds into A and M
+// (14 FMA-pipe operations instead of 17 for kl x r scaled and summed); the cross product with
+// q - o is taken once per sub-block.  The sub-block origin keeps |q - o| within the
+// sub-block's extent of |r|, so the cancellation in A x (q - o) - M costs no more than the
+// rounding of r itself.  Pair terms run as packed FP32 pairs (PTX f32x2, two segments per
+// instruction), rsqrt on the MUFU pipe; each half accumulates its 32 segments of a sub-block
+// in FP32, the sub-block's field is added to a Kahan-compensated (S, C) pair, and S - C is
+// taken in FP64 at the end.
 #pragma once
 
 #include <stdint.h>
@@ -60,7 +69,11 @@ __device__ __forceinline__ void kahan_add(float &S, float &C, float s) {
 struct TileHeader {
     float o_hi[3], o_lo[3];
     int count, pad;
+    float sub_o[kTile / kSub][3];
+    float pad2[2];
 };
+static_assert(sizeof(TileHeader) == kTileHeaderBytes, "tile header layout");
+static_assert(kTile == 2 * kSub, "two sub-blocks per tile");
 
 // Per-point state of the compensated sum.
 template <int PPT>
@@ -126,23 +139,27 @@ __device__ __forceinline__ void tile_f32c_smem(const unsigned char *tile, const 
 template <int PPT, int JU>
 __device__ __forceinline__ void tile_pairs(const unsigned char *tile, const f2 (&q)[PPT][3], F32cAcc<PPT> &acc,
                                            int g0, int g1) {
+    const TileHeader *h = reinterpret_cast<const TileHeader *>(tile);
     const ulonglong2 *v = reinterpret_cast<const ulonglong2 *>(tile + kTileHeaderBytes);
-    constexpr int Q = kTile / 4;   // ulonglong2 (4 floats) per component array
+    constexpr int Q = kTile / 4;          // ulonglong2 (4 floats) per component array
+    constexpr int SG = kSub / 4;          // 4-segment groups per sub-block
+    // g0 and g1 are multiples of SG (whole sub-blocks)
 #pragma unroll 1
-    for (int sb = g0; sb < g1; sb += 16) {                       // sub-blocks of <= 64 segments
-        const int se = min(sb + 16, g1);
-        f2 B[PPT][3];
+    for (int sb = g0; sb < g1; sb += SG) {
+        f2 A[PPT][3], M[PPT][3];
 #pragma unroll
-        for (int i = 0; i < PPT; ++i) B[i][0] = B[i][1] = B[i][2] = 0ull;
+        for (int i = 0; i < PPT; ++i)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) A[i][c] = M[i][c] = 0ull;
 #pragma unroll JU
-        for (int j = sb; j < se; ++j) {                          // 4 segments per iteration
+        for (int j = sb; j < sb + SG; ++j) {                     // 4 segments per iteration
             const ulonglong2 KX = v[0 * Q + j], KY = v[1 * Q + j], KZ = v[2 * Q + j];
-            const ulonglong2 NX = v[3 * Q + j], NY = v[4 * Q + j], NZ = v[5 * Q + j];
+            const ulonglong2 MX = v[3 * Q + j], MY = v[4 * Q + j], MZ = v[5 * Q + j];
             const ulonglong2 PX = v[6 * Q + j], PY = v[7 * Q + j], PZ = v[8 * Q + j];
 #pragma unroll
             for (int hh = 0; hh < 2; ++hh) {
                 const f2 kx = hh ? KX.y : KX.x, ky = hh ? KY.y : KY.x, kz = hh ? KZ.y : KZ.x;
-                const f2 nx = hh ? NX.y : NX.x, ny = hh ? NY.y : NY.x, nz = hh ? NZ.y : NZ.x;
+                const f2 mx = hh ? MX.y : MX.x, my = hh ? MY.y : MY.x, mz = hh ? MZ.y : MZ.x;
                 const f2 px = hh ? PX.y : PX.x, py = hh ? PY.y : PY.x, pz = hh ? PZ.y : PZ.x;
 #pragma unroll
                 for (int i = 0; i < PPT; ++i) {
@@ -152,24 +169,34 @@ __device__ __forceinline__ void tile_pairs(const unsigned char *tile, const f2 (
                     f2_unpack(r2, a, b);
                     const f2 inv = f2_pack(rsqrt_mufu(a), rsqrt_mufu(b));
                     const f2 inv3 = f2_mul(f2_mul(inv, inv), inv);
-                    // kl x r = (ky rz - kz ry, kz rx - kx rz, kx ry - ky rx)
-                    const f2 cx = f2_fma(ky, rz, f2_mul(nz, ry));
-                    const f2 cy = f2_fma(kz, rx, f2_mul(nx, rz));
-                    const f2 cz = f2_fma(kx, ry, f2_mul(ny, rx));
-                    B[i][0] = f2_fma(cx, inv3, B[i][0]);
-                    B[i][1] = f2_fma(cy, inv3, B[i][1]);
-                    B[i][2] = f2_fma(cz, inv3, B[i][2]);
+                    A[i][0] = f2_fma(kx, inv3, A[i][0]);
+                    A[i][1] = f2_fma(ky, inv3, A[i][1]);
+                    A[i][2] = f2_fma(kz, inv3, A[i][2]);
+                    M[i][0] = f2_fma(mx, inv3, M[i][0]);
+                    M[i][1] = f2_fma(my, inv3, M[i][1]);
+                    M[i][2] = f2_fma(mz, inv3, M[i][2]);
                 }
             }
         }
+        const float *o = h->sub_o[sb / SG];
 #pragma unroll
-        for (int i = 0; i < PPT; ++i)
+        for (int i = 0; i < PPT; ++i) {
+            float a[3], m[3], w[3];
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
                 float lo, hi;
-                f2_unpack(B[i][c], lo, hi);
-                kahan_add(acc.S[i][c], acc.C[i][c], __fadd_rn(lo, hi));
+                f2_unpack(A[i][c], lo, hi);
+                a[c] = __fadd_rn(lo, hi);
+                f2_unpack(M[i][c], lo, hi);
+                m[c] = __fadd_rn(lo, hi);
+                f2_unpack(q[i][c], lo, hi);
+                w[c] = __fsub_rn(lo, o[c]);
             }
+            // A x w - M
+            kahan_add(acc.S[i][0], acc.C[i][0], __fmaf_rn(a[1], w[2], __fmaf_rn(-a[2], w[1], -m[0])));
+            kahan_add(acc.S[i][1], acc.C[i][1], __fmaf_rn(a[2], w[0], __fmaf_rn(-a[0], w[2], -m[1])));
+            kahan_add(acc.S[i][2], acc.C[i][2], __fmaf_rn(a[0], w[1], __fmaf_rn(-a[1], w[0], -m[2])));
+        }
     }
 }
 
@@ -193,7 +220,7 @@ __device__ __forceinline__ void tile_grad_f32c(const unsigned char *tile, const 
     const TileHeader *h = reinterpret_cast<const TileHeader *>(tile);
     const ulonglong2 *v = reinterpret_cast<const ulonglong2 *>(tile + kTileHeaderBytes);
     constexpr int Q = kTile / 4;
-    f2 q[PPT][3], A[PPT][3];
+    f2 q[PPT][3], A[PPT][3], NA[PPT][3];
 #pragma unroll
     for (int i = 0; i < PPT; ++i)
 #pragma unroll
@@ -201,6 +228,7 @@ __device__ __forceinline__ void tile_grad_f32c(const unsigned char *tile, const 
             const float d = __fadd_rn(__fsub_rn(ph[i][c], h->o_hi[c]), __fsub_rn(pl[i][c], h->o_lo[c]));
             q[i][c] = f2_pack(d, d);
             A[i][c] = f2_pack(a[i][c], a[i][c]);
+            NA[i][c] = f2_pack(-a[i][c], -a[i][c]);
         }
     const f2 m3 = f2_pack(-3.0f, -3.0f);
 #pragma unroll 1
@@ -212,12 +240,10 @@ __device__ __forceinline__ void tile_grad_f32c(const unsigned char *tile, const 
 #pragma unroll 1
         for (int j = sb; j < se; ++j) {
             const ulonglong2 KX = v[0 * Q + j], KY = v[1 * Q + j], KZ = v[2 * Q + j];
-            const ulonglong2 NX = v[3 * Q + j], NY = v[4 * Q + j], NZ = v[5 * Q + j];
             const ulonglong2 PX = v[6 * Q + j], PY = v[7 * Q + j], PZ = v[8 * Q + j];
 #pragma unroll
             for (int hh = 0; hh < 2; ++hh) {
                 const f2 kx = hh ? KX.y : KX.x, ky = hh ? KY.y : KY.x, kz = hh ? KZ.y : KZ.x;
-                const f2 nx = hh ? NX.y : NX.x, ny = hh ? NY.y : NY.x, nz = hh ? NZ.y : NZ.x;
                 const f2 px = hh ? PX.y : PX.x, py = hh ? PY.y : PY.x, pz = hh ? PZ.y : PZ.x;
 #pragma unroll
                 for (int i = 0; i < PPT; ++i) {
@@ -230,9 +256,9 @@ __device__ __forceinline__ void tile_grad_f32c(const unsigned char *tile, const 
                     const f2 inv3 = f2_mul(inv2, inv);
                     const f2 m3inv5 = f2_mul(f2_mul(inv3, inv2), m3);
                     // c = a x kl = (ay kz - az ky, az kx - ax kz, ax ky - ay kx)
-                    const f2 cx = f2_fma(A[i][1], kz, f2_mul(A[i][2], ny));
-                    const f2 cy = f2_fma(A[i][2], kx, f2_mul(A[i][0], nz));
-                    const f2 cz = f2_fma(A[i][0], ky, f2_mul(A[i][1], nx));
+                    const f2 cx = f2_fma(A[i][1], kz, f2_mul(NA[i][2], ky));
+                    const f2 cy = f2_fma(A[i][2], kx, f2_mul(NA[i][0], kz));
+                    const f2 cz = f2_fma(A[i][0], ky, f2_mul(NA[i][1], kx));
                     const f2 cr = f2_fma(cx, rx, f2_fma(cy, ry, f2_mul(cz, rz)));
                     const f2 nq = f2_mul(cr, m3inv5);
                     G[i][0] = f2_fma(nq, rx, f2_fma(cx, inv3, G[i][0]));

@@ -12,6 +12,7 @@ namespace cctgpu {
 constexpr int kTrackBlock = 64;      // 2 warps; 8 CTAs per SM, which take units dynamically
 constexpr int kTrackMinBlocks = 8;
 constexpr int kTrackWarps = kTrackBlock / 32;
+static_assert((kTile / kTrackWarps) % kSub == 0, "tile slices hold whole FP32c sub-blocks");
 constexpr int kMaxGroup = 64 * kTrackWarps;   // particles per unit: 2 per lane in every warp
 constexpr int kStateD = 24;          // doubles of RK4 state per particle
 constexpr int kMaxChunks = 4096;     // chunks per (design, block)
