@@ -10,9 +10,9 @@ namespace cctgpu {
 
 // ---------------------------------------------------------------- constants
 constexpr int kTile = 128;                   // segments per FP32c tile
-constexpr int kSub = 64;                     // segments per FP32c sub-block (own moment origin)
-constexpr int kTileHeaderBytes = 64;         // double-float origin, count, pad, sub-block origins
-constexpr int kTileBytes = kTileHeaderBytes + 9 * kTile * 4;   // 4672, a multiple of 16
+constexpr int kSub = 32;                     // segments per FP32c sub-block (own moment origin)
+constexpr int kTileHeaderBytes = 96;         // double-float origin, count, pad, sub-block origins
+constexpr int kTileBytes = kTileHeaderBytes + 9 * kTile * 4;   // 4704, a multiple of 16
 constexpr int kPackedHeaderBytes = 256;      // magic, n_designs, n_tiles
 constexpr int64_t kPackedMagic = 0x4343543332434332LL;          // "CCT32CC2"
 constexpr float kPadOffset = 1.0e18f;        // padding segment: kl = 0, far away

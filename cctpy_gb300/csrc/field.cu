@@ -10,7 +10,7 @@
 //                       carries a double-float origin, point-minus-origin is taken in
 //                       double-float, the pair terms run as packed FP32x2 (two segments
 //                       per instruction; rsqrt on the MUFU pipe) in the moment form
-//                       (sums of kl |r|^-3 and (kl x p0) |r|^-3 per 64-segment
+//                       (sums of kl |r|^-3 and (kl x p0) |r|^-3 per 32-segment
 //                       sub-block, crossed with the point once per sub-block), summed into
 //                       a Kahan-compensated (S, C) pair resolved in FP64 at the end
 //                       (tile.cuh).  Tiles are streamed into
@@ -115,7 +115,7 @@ int launch_field_f64(const double *kls, const double *p0s, int64_t n_seg, const 
 // Packs FP64 segments into FP32c tiles (layout in tile.cuh).  The tile origin is the
 // centroid of the tile's midpoints rounded to a double-float (hi, lo) pair; offsets are
 // taken from that represented origin, so point - origin needs no FP64 in the kernels.  Each
-// 64-segment sub-block gets its own FP32 origin (centroid of its offsets), about which the
+// 32-segment sub-block gets its own FP32 origin (centroid of its offsets), about which the
 // moments kl x (p0 - origin - sub-block origin) are formed in FP64 and rounded once.
 __global__ void __launch_bounds__(kTile) pack_f32c_kernel(const double *__restrict__ kls,
                                                           const double *__restrict__ p0s,
@@ -194,7 +194,8 @@ __global__ void __launch_bounds__(kTile) pack_f32c_kernel(const double *__restri
         }
         hdr->count = cnt;
         hdr->pad = 0;
-        hdr->pad2[0] = hdr->pad2[1] = 0.0f;
+#pragma unroll
+        for (int c = 0; c < 4; ++c) hdr->pad2[c] = 0.0f;
     }
     if (i % kSub == 0) {
 #pragma unroll
@@ -250,11 +251,15 @@ int launch_pack_f32c(const double *kls, const double *p0s, const int64_t *h_seg_
 }
 
 // ===================================================================== FP32c field
-constexpr int kF32Block = 128;   // 4 CTAs per SM: measured faster than 2 x 256 on GB300
-constexpr int kF32Ppt = 2;
-constexpr int kF32Blocks = 4;
-constexpr int kF32Unroll = 2;
-constexpr int kStages = 4;
+// Launch shape from a sweep of (threads, points per thread, CTAs per SM, unroll, ring depth)
+// on the 2^20-point field map: 3 points per thread, 3 CTAs of 4 warps per SM (146 registers),
+// the sub-block's 8-iteration segment loop fully unrolled.  CTAs of 3 or 6 warps were 20 %
+// slower (their warps leave one SM sub-partition idle).
+constexpr int kF32Block = 128;
+constexpr int kF32Ppt = 3;
+constexpr int kF32Blocks = 3;
+constexpr int kF32Unroll = 8;
+constexpr int kStages = 3;
 constexpr uint32_t kWaitPolls = 1u << 22;
 
 __device__ int g_field_status;   // last non-OK status seen by a field kernel (sticky)

@@ -1,9 +1,9 @@
 // One FP32-compensated tile of the packed segment form, shared by the field-map and
 // tracking kernels.
 //
-// Tile (kTileBytes = 4672 = 16 * 292):
+// Tile (kTileBytes = 4704 = 16 * 294):
 //   float o_hi[3], o_lo[3];  int count; int pad;      origin = o_hi + o_lo (double-float)
-//   float sub_o[2][3]; float pad2[2];                 origin of each 64-segment sub-block,
+//   float sub_o[4][3]; float pad2[4];                 origin of each 32-segment sub-block,
 //                                                     relative to the tile origin
 //   float kx[128], ky[128], kz[128];                   kl
 //   float mx[128], my[128], mz[128];                   kl x (p0 - origin - sub_o)
@@ -14,11 +14,13 @@
 // so a pair costs r = q - p_i, |r|^2, rsqrt, |r|^-3 and the six multiply-adds into A and M
 // (14 FMA-pipe operations instead of 17 for kl x r scaled and summed); the cross product with
 // q - o is taken once per sub-block.  The sub-block origin keeps |q - o| within the
-// sub-block's extent of |r|, so the cancellation in A x (q - o) - M costs no more than the
-// rounding of r itself.  Pair terms run as packed FP32 pairs (PTX f32x2, two segments per
-// instruction), rsqrt on the MUFU pipe; each half accumulates its 32 segments of a sub-block
-// in FP32, the sub-block's field is added to a Kahan-compensated (S, C) pair, and S - C is
-// taken in FP64 at the end.
+// sub-block's extent of |r|, so the cancellation in A x (q - o) - M adds little to the
+// rounding of r itself (measured by an FP32 emulation: at points 3-8 mm from the windings
+// 1.3x the error of the direct form with 32-segment sub-blocks, 1.85x with 64).  Pair terms
+// run as packed FP32 pairs (PTX f32x2, two segments per instruction), rsqrt on the MUFU pipe;
+// each half accumulates A over the 16 segments of a sub-block and M over the whole call (a
+// tile or a slice of it) in FP32; the call's field sum(A x w) - M is added to a
+// Kahan-compensated (S, C) pair, and S - C is taken in FP64 at the end.
 #pragma once
 
 #include <stdint.h>
@@ -70,10 +72,10 @@ struct TileHeader {
     float o_hi[3], o_lo[3];
     int count, pad;
     float sub_o[kTile / kSub][3];
-    float pad2[2];
+    float pad2[4];
 };
 static_assert(sizeof(TileHeader) == kTileHeaderBytes, "tile header layout");
-static_assert(kTile == 2 * kSub, "two sub-blocks per tile");
+static_assert(kTile == 4 * kSub, "four sub-blocks per tile");
 
 // Per-point state of the compensated sum.
 template <int PPT>
@@ -143,14 +145,22 @@ __device__ __forceinline__ void tile_pairs(const unsigned char *tile, const f2 (
     const ulonglong2 *v = reinterpret_cast<const ulonglong2 *>(tile + kTileHeaderBytes);
     constexpr int Q = kTile / 4;          // ulonglong2 (4 floats) per component array
     constexpr int SG = kSub / 4;          // 4-segment groups per sub-block
-    // g0 and g1 are multiples of SG (whole sub-blocks)
+    // g0 and g1 are multiples of SG (whole sub-blocks).  T collects the sub-blocks' A x w;
+    // the moments M of all sub-blocks of the call are summed together and subtracted once.
+    float T[PPT][3];
+    f2 M[PPT][3];
+#pragma unroll
+    for (int i = 0; i < PPT; ++i)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            T[i][c] = 0.0f;
+            M[i][c] = 0ull;
+        }
 #pragma unroll 1
     for (int sb = g0; sb < g1; sb += SG) {
-        f2 A[PPT][3], M[PPT][3];
+        f2 A[PPT][3];
 #pragma unroll
-        for (int i = 0; i < PPT; ++i)
-#pragma unroll
-            for (int c = 0; c < 3; ++c) A[i][c] = M[i][c] = 0ull;
+        for (int i = 0; i < PPT; ++i) A[i][0] = A[i][1] = A[i][2] = 0ull;
 #pragma unroll JU
         for (int j = sb; j < sb + SG; ++j) {                     // 4 segments per iteration
             const ulonglong2 KX = v[0 * Q + j], KY = v[1 * Q + j], KZ = v[2 * Q + j];
@@ -181,23 +191,29 @@ __device__ __forceinline__ void tile_pairs(const unsigned char *tile, const f2 (
         const float *o = h->sub_o[sb / SG];
 #pragma unroll
         for (int i = 0; i < PPT; ++i) {
-            float a[3], m[3], w[3];
+            float a[3], w[3];
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
                 float lo, hi;
                 f2_unpack(A[i][c], lo, hi);
                 a[c] = __fadd_rn(lo, hi);
-                f2_unpack(M[i][c], lo, hi);
-                m[c] = __fadd_rn(lo, hi);
                 f2_unpack(q[i][c], lo, hi);
                 w[c] = __fsub_rn(lo, o[c]);
             }
-            // A x w - M
-            kahan_add(acc.S[i][0], acc.C[i][0], __fmaf_rn(a[1], w[2], __fmaf_rn(-a[2], w[1], -m[0])));
-            kahan_add(acc.S[i][1], acc.C[i][1], __fmaf_rn(a[2], w[0], __fmaf_rn(-a[0], w[2], -m[1])));
-            kahan_add(acc.S[i][2], acc.C[i][2], __fmaf_rn(a[0], w[1], __fmaf_rn(-a[1], w[0], -m[2])));
+            // T += A x w
+            T[i][0] = __fmaf_rn(a[1], w[2], __fmaf_rn(-a[2], w[1], T[i][0]));
+            T[i][1] = __fmaf_rn(a[2], w[0], __fmaf_rn(-a[0], w[2], T[i][1]));
+            T[i][2] = __fmaf_rn(a[0], w[1], __fmaf_rn(-a[1], w[0], T[i][2]));
         }
     }
+#pragma unroll
+    for (int i = 0; i < PPT; ++i)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            float lo, hi;
+            f2_unpack(M[i][c], lo, hi);
+            kahan_add(acc.S[i][c], acc.C[i][c], __fsub_rn(T[i][c], __fadd_rn(lo, hi)));
+        }
 }
 
 // Split an FP64 coordinate into a double-float (hi, lo) pair.

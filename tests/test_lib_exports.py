@@ -40,7 +40,7 @@ def test_host_only_calls(lib):
     assert lib.cct_f32c_tile() == 128
     off = (ctypes.c_int64 * 3)(0, 46080, 46081)
     n = lib.cct_f32c_packed_bytes(ctypes.cast(off, ctypes.c_void_p), 2)
-    assert n == 256 + 256 + (360 + 1) * 4672
+    assert n == 256 + 256 + (360 + 1) * 4704
     assert lib.cct_track_scratch_bytes(1, 32) > 0
     # argument errors are reported without touching the GPU
     assert lib.cct_track_scratch_bytes(0, 32) == -1
