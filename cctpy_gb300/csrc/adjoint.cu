@@ -346,6 +346,7 @@ __global__ void __launch_bounds__(kSegBlock) seg_adjoint_kernel(TrackParams P, i
 // segment.
 constexpr int kSegPts = 128;
 constexpr int kSegThreads = 64;
+constexpr int kSegUnroll = 4;
 
 __global__ void seg_prep_kernel(const double *__restrict__ record, int64_t n_rec, float4 *__restrict__ out) {
     for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n_rec; e += (int64_t)gridDim.x * blockDim.x) {
@@ -361,7 +362,8 @@ __global__ void seg_prep_kernel(const double *__restrict__ record, int64_t n_rec
 __global__ void __launch_bounds__(kSegThreads, 8) seg_adjoint_f32c_kernel(TrackParams P, int n_steps,
                                                                           const float4 *__restrict__ pts_df,
                                                                           double *grad) {
-    __shared__ __align__(16) f2 pts[kSegPts][9];   // (q,q) x3, (a,a) x3, (n,n) x3 with n = q x a
+    // per point, as packed pairs (v, v): a x3, q x3, n x3 with n = q x a, pad (80 B: five 16-byte loads)
+    __shared__ __align__(16) f2 pts[kSegPts][10];
     const int64_t t = blockIdx.x;
     int lo = 0, hi = P.n_designs - 1;               // design of tile t: last d with tile_off[d] <= t
     while (lo < hi) {
@@ -405,23 +407,31 @@ __global__ void __launch_bounds__(kSegThreads, 8) seg_adjoint_f32c_kernel(TrackP
                 a[1] = w.w;
                 a[2] = z.x;
             }
+            if (a[0] == 0.0f && a[1] == 0.0f && a[2] == 0.0f) {
+                // no weight (an inactive stage, or past the last point): park the point far
+                // away (opposite the padding segments), so that its terms are exactly zero
+                // and the pair loop needs no branch
+                q[0] = q[1] = q[2] = -kPadOffset;
+            }
             const float n[3] = {__fmaf_rn(q[1], a[2], -q[2] * a[1]), __fmaf_rn(q[2], a[0], -q[0] * a[2]),
                                 __fmaf_rn(q[0], a[1], -q[1] * a[0])};
             for (int c = 0; c < 3; ++c) {
-                pts[k][c] = f2_pack(q[c], q[c]);
-                pts[k][3 + c] = f2_pack(a[c], a[c]);
+                pts[k][c] = f2_pack(a[c], a[c]);
+                pts[k][3 + c] = f2_pack(q[c], q[c]);
                 pts[k][6 + c] = f2_pack(n[c], n[c]);
             }
+            pts[k][9] = 0ull;
         }
         __syncthreads();
         f2 V[3] = {0ull, 0ull, 0ull}, W[3] = {0ull, 0ull, 0ull}, U[3] = {0ull, 0ull, 0ull}, T = 0ull;
         const int np = (int)min((int64_t)kSegPts, n_pts - base);
-#pragma unroll 2
+#pragma unroll kSegUnroll
         for (int i = 0; i < np; ++i) {
-            const f2 Ax = pts[i][3], Ay = pts[i][4], Az = pts[i][5];
-            if ((Ax | Ay | Az) == 0ull) continue;              // inactive stage: uniform over the CTA
-            const f2 Qx = pts[i][0], Qy = pts[i][1], Qz = pts[i][2];
-            const f2 Nx = pts[i][6], Ny = pts[i][7], Nz = pts[i][8];
+            const ulonglong2 *row = reinterpret_cast<const ulonglong2 *>(pts[i]);
+            const ulonglong2 v0 = row[0], v1 = row[1], v2 = row[2], v3 = row[3], v4 = row[4];
+            const f2 Ax = v0.x, Ay = v0.y, Az = v1.x;
+            const f2 Qx = v1.y, Qy = v2.x, Qz = v2.y;
+            const f2 Nx = v3.x, Ny = v3.y, Nz = v4.x;
             const f2 rx = f2_sub(Qx, px), ry = f2_sub(Qy, py), rz = f2_sub(Qz, pz);
             const f2 r2 = f2_fma(rx, rx, f2_fma(ry, ry, f2_mul(rz, rz)));
             float l0, l1;

@@ -19,6 +19,7 @@ constexpr int kMaxChunks = 4096;     // chunks per (design, block)
 constexpr int kUnitsPerCta = 8;      // default target units per CTA and stage (dynamic load balance)
 constexpr int kRing = 4;             // TMA ring depth (tiles)
 constexpr int kTrackUnroll = 8;      // unroll of the 4-segment loop of a sub-block (8: fully)
+constexpr int kGradUnroll = 4;       // the same in the adjoint's gradient sums
 constexpr int kRedDoubles = kMaxGroup * 3;   // per-CTA reduction buffer: S slices x G particles x 3
 constexpr uint32_t kTmaPolls = 1u << 22;
 
@@ -304,7 +305,7 @@ static __device__ int64_t unit_sum_f32c(const TrackParams &P, const PointSrc &sr
             ok_all = false;
             break;
         }
-        if (GRAD) tile_grad_f32c<PPT>(sm.ring[s], ph, pl, a, acc, g0, g1);
+        if (GRAD) tile_grad_f32c<PPT, kGradUnroll>(sm.ring[s], ph, pl, a, acc, g0, g1);
         else tile_f32c<PPT, kTrackUnroll>(sm.ring[s], ph, pl, acc, g0, g1);
         if (cctdev::ring_release_last(&sm.released[s], kTrackWarps) && t + kRing < nt) {
             sm.last_issued[s] = k + kRing;
