@@ -37,7 +37,7 @@ FLOPS_PER_PAIR = 26
 # dram__bytes_read.sum + dram__bytes_write.sum of one field_f32c_kernel launch on the field map
 # (ncu --section MemoryWorkloadAnalysis ...; profiles/field_f32c_field_map.md): the 25 MB of
 # points and 1.7 MB of tiles read; the 25 MB of fields written are still in L2 at the end.
-FIELD_MAP_TRAFFIC_BYTES = 27.3e6
+FIELD_MAP_TRAFFIC_BYTES = 26.96e6
 METRIC = "Biot-Savart Gpairs/s & design-grads/s, 1 GB300: FP32+comp vs FP64 @1e-7 rel"
 WORKLOAD = "field_map: 2^20 points x 46080-segment single CCT dipole"
 
