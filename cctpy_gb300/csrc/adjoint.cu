@@ -522,7 +522,7 @@ static int adjoint_grid(int *grid_out) {
 
 static int64_t adjoint_scratch_bound(int n_designs, int64_t n_p, int max_steps, int K) {
     const int64_t track = track_scratch_bound(n_designs, n_p);
-    TrackScratchLayout L{0, 0, 0, track};
+    TrackScratchLayout L{0, 0, 0, 0, track};
     const int n_ckpt = (max_steps + K - 1) / K;
     return adj_layout(L, n_designs, n_p, n_ckpt, K).total;
 }
@@ -588,6 +588,7 @@ static int launch_adjoint(const double *kls, const double *p0s, const int64_t *s
     P.barrier_blocks = (unsigned)(grid + g_test_phantom_blocks);
     P.wait_ns = (unsigned long long)g_wait_ms * 1000000ull;
     P.record = nullptr;
+    set_flow(P, sc + L.flow_off);   // the forward launches; the reverse sweep keeps its barriers
 
     // 1. state from the records; learn the step count
     CCT_TRY_CUDA(cudaMemsetAsync(sc, 0, 256, st));

@@ -44,7 +44,7 @@ int launch_field_f32c(const void *packed, int design, const double *qs, int n_qs
                       int64_t n, double *B, cudaStream_t st);
 
 struct TrackScratchLayout {
-    int64_t state_off, partial_off, ctrl_off, total;
+    int64_t state_off, partial_off, ctrl_off, flow_off, total;
 };
 // Scratch layout for n_units units of `group` particles each.
 TrackScratchLayout track_scratch_layout(int n_designs, int64_t n_particles, int64_t n_units, int group);

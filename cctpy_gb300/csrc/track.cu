@@ -29,6 +29,46 @@
 
 namespace cctgpu {
 
+// Dataflow schedule, FP32c: the CTA walks the launch's unit sequence; before a unit it waits
+// until the unit's particle block has finished the previous stage, after it counts the unit
+// done, and the CTA that finishes a block's stage runs that block's particle update.
+// Returns false if a wait gave up (CCT_ERR_TIMEOUT recorded, ring drained).
+template <int PPT>
+static __device__ bool flow_f32c(const TrackParams &P, TrackSmem &sm, uint32_t &kt, int64_t n_units, int64_t n_seq) {
+    int64_t s = first_unit();
+    if (s < n_seq) unit_prefetch(P, s % n_units, sm, kt);
+    while (s < n_seq) {
+        const int k = (int)(s / n_units);
+        const int64_t u = s % n_units;
+        const UnitRef U = locate_unit(P, u);
+        const int64_t blk = (int64_t)U.d * P.blocks + U.b;
+        if (!flow_wait(P, sm, blk, k)) {
+            if (threadIdx.x == 0) ring_drain(sm);   // the unit's first tiles are in flight
+            __syncthreads();
+            return false;
+        }
+        if (unit_sum_f32c<PPT, false, true>(P, stage_points(P), u, sm, kt, k, n_units, n_seq) < 0) return false;
+        if (flow_complete(P, sm, blk, k, P.chunks[U.d])) block_update(P, U.d, U.b, k);
+        s = claim_seq(P, sm);
+        if (s < n_seq) unit_prefetch(P, s % n_units, sm, kt);
+    }
+    return true;
+}
+
+// The same for FP64 units (no tile ring).
+static __device__ bool flow_f64(const TrackParams &P, TrackSmem &sm, int64_t n_units, int64_t n_seq) {
+    for (int64_t s = first_unit(); s < n_seq; s = claim_seq(P, sm)) {
+        const int k = (int)(s / n_units);
+        const int64_t u = s % n_units;
+        const UnitRef U = locate_unit(P, u);
+        const int64_t blk = (int64_t)U.d * P.blocks + U.b;
+        if (!flow_wait(P, sm, blk, k)) return false;
+        unit_field_f64(P, u, sm);
+        if (flow_complete(P, sm, blk, k, P.chunks[U.d])) block_update(P, U.d, U.b, k);
+    }
+    return true;
+}
+
 __global__ void __launch_bounds__(kTrackBlock, kTrackMinBlocks) track_kernel(TrackParams P) {
     __shared__ __align__(128) TrackSmem sm;
     const int64_t total = (int64_t)P.n_designs * P.n_p;
@@ -62,8 +102,15 @@ __global__ void __launch_bounds__(kTrackBlock, kTrackMinBlocks) track_kernel(Tra
     const int64_t gwarp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
 
+    if (P.use_flow) {
+        const int64_t n_seq = step_end > P.step_begin ? (int64_t)(step_end - P.step_begin) * 4 * n_units : 0;
+        if (P.precision == 0) (void)flow_f64(P, sm, n_units, n_seq);
+        else if (P.ppt == 2) (void)flow_f32c<2>(P, sm, kt, n_units, n_seq);
+        else (void)flow_f32c<1>(P, sm, kt, n_units, n_seq);
+        if (!grid_barrier(P, sm)) return;   // every stage of every block is done (or a wait gave up)
+    }
     int phase = 0;
-    for (int step = P.step_begin; step < step_end; ++step) {
+    for (int step = P.step_begin; !P.use_flow && step < step_end; ++step) {
         for (int stage = 0; stage < 4; ++stage, ++phase) {
             if (P.precision == 0) {
                 for (int64_t u = first_unit(); u < n_units; u = next_unit(P, sm, phase))
@@ -109,7 +156,8 @@ TrackScratchLayout track_scratch_layout(int n_designs, int64_t n_particles, int6
     L.ctrl_off = 0;
     L.state_off = 256 + tables;
     L.partial_off = L.state_off + up(8 * kStateD * (int64_t)n_designs * n_particles);
-    L.total = L.partial_off + up(24 * (int64_t)group * n_units);
+    L.flow_off = L.partial_off + up(24 * (int64_t)group * n_units);
+    L.total = L.flow_off + up(kFlowBytesPerBlock * (int64_t)n_designs * ((n_particles + group - 1) / group));
     return L;
 }
 
@@ -135,6 +183,16 @@ int track_grid(int *grid_out) {
 }
 
 int g_units_per_cta = kUnitsPerCta;
+
+// Dataflow schedule for batches of at least kFlowMinBlocks particle blocks (their stage
+// particle updates overlap other blocks' field sums); smaller batches keep the two grid
+// barriers per stage, whose particle update runs on every CTA at once.
+void set_flow(TrackParams &P, unsigned char *flow) {
+    P.blocks = (P.n_p + P.G - 1) / P.G;
+    P.use_flow = (int64_t)P.n_designs * P.blocks >= kFlowMinBlocks ? 1 : 0;
+    P.flow_done = reinterpret_cast<unsigned long long *>(flow);
+    P.flow_ready = reinterpret_cast<unsigned *>(flow + 8 * (int64_t)P.n_designs * P.blocks);
+}
 
 int64_t plan_units(const int64_t *hoff, int n_designs, int64_t n_p, int G, int grid, int64_t max_units,
                    int64_t *unit_off, int64_t *chunks, int64_t *chunk_tiles) {
@@ -247,6 +305,7 @@ static int run_track(const double *kls, const double *p0s, const int64_t *seg_of
     P.step_begin = 0;
     P.step_end = 0x7fffffff;
     P.record = nullptr;
+    set_flow(P, sc + L.flow_off);
     CCT_TRY_CUDA(launch_track_kernel(P, grid, st));
 
     unsigned ctrl[8];
@@ -361,6 +420,7 @@ int launch_track_async(const double *kls, const double *p0s, const int64_t *seg_
     P.step_begin = 0;
     P.step_end = 0x7fffffff;
     P.record = nullptr;
+    set_flow(P, sc + L.flow_off);
     CCT_TRY_CUDA(cudaMemsetAsync(sc, 0, 256, st));
     plan_kernel<<<1, 32, 0, st>>>(P, static_cast<const unsigned char *>(packed), (int64_t)g_units_per_cta * grid,
                                   max_units, reinterpret_cast<int64_t *>(sc + 256));

@@ -23,8 +23,13 @@ constexpr int kGradUnroll = 4;       // the same in the adjoint's gradient sums
 constexpr int kRedDoubles = kMaxGroup * 3;   // per-CTA reduction buffer: S slices x G particles x 3
 constexpr uint32_t kTmaPolls = 1u << 22;
 
-// control words
-enum { CW_COUNT = 0, CW_GEN = 1, CW_ERR = 2, CW_NONFINITE = 3, CW_MAXSTEPS = 4, CW_NEXT0 = 5, CW_NEXT1 = 6 };
+// control words (CW_SEQ: a 64-bit counter in words 8-9)
+enum { CW_COUNT = 0, CW_GEN = 1, CW_ERR = 2, CW_NONFINITE = 3, CW_MAXSTEPS = 4, CW_NEXT0 = 5, CW_NEXT1 = 6, CW_SEQ = 8 };
+
+// Dataflow schedule (batches of at least kFlowMinBlocks particle blocks): per particle block a
+// 64-bit count of finished chunk units and a 32-bit count of finished stages.
+constexpr int kFlowMinBlocks = 8;
+constexpr int kFlowBytesPerBlock = 16;
 
 // state layout per particle
 enum { ST_Y0 = 0, ST_YS = 6, ST_KSUM = 12, ST_DT = 18, ST_KQ = 19, ST_NSTEPS = 20 };
@@ -55,6 +60,11 @@ struct TrackParams {
     int write_back;                // 1: write the final state into the particle records
     int step_begin, step_end;      // steps [step_begin, min(step_end, step count)) run here
     double *record;                // null, or per (step, stage, particle): stage state + field
+    // dataflow schedule (use_flow = 1): per particle block (design d, block b at d * blocks + b)
+    int use_flow;
+    int64_t blocks;                // particle blocks per design
+    unsigned long long *flow_done; // units finished, all stages of this launch
+    unsigned *flow_ready;          // stages whose particle update is complete
 };
 
 // record entry of one (step, stage, particle): stage Y (6), B at the stage position (3),
@@ -138,6 +148,16 @@ static __device__ __forceinline__ int64_t next_unit(const TrackParams &P, TrackS
     __syncthreads();
     return sm.unit;
 }
+// Dataflow schedule: one sequence over all stages of the launch, unit u of stage k at
+// k * n_units + u.  CTA b first takes b, further entries come from the 64-bit counter CW_SEQ.
+static __device__ __forceinline__ int64_t claim_seq(const TrackParams &P, TrackSmem &sm) {
+    __syncthreads();
+    if (threadIdx.x == 0)
+        sm.unit = (int64_t)gridDim.x +
+                  (int64_t)atomicAdd(reinterpret_cast<unsigned long long *>(P.ctrl + CW_SEQ), 1ull);
+    __syncthreads();
+    return sm.unit;
+}
 static __device__ __forceinline__ void reset_next_unit(const TrackParams &P, int phase) {
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicExch(P.ctrl + CW_NEXT0 + ((phase + 1) & 1), 0u);
 }
@@ -146,7 +166,68 @@ static __device__ __forceinline__ void clear_unit_counters(const TrackParams &P)
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         atomicExch(P.ctrl + CW_NEXT0, 0u);
         atomicExch(P.ctrl + CW_NEXT1, 0u);
+        atomicExch(reinterpret_cast<unsigned long long *>(P.ctrl + CW_SEQ), 0ull);
     }
+    if (P.use_flow) {
+        const int64_t n_blk = (int64_t)P.n_designs * P.blocks;
+        for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n_blk; i += (int64_t)gridDim.x * blockDim.x) {
+            P.flow_done[i] = 0ull;
+            P.flow_ready[i] = 0u;
+        }
+    }
+}
+
+// Thread 0, after a wait gave up: let the last copy into every ring slot land before the
+// CTA's shared memory is given up (earlier copies into a slot were consumed before its refill).
+static __device__ void ring_drain(TrackSmem &sm) {
+    for (int s = 0; s < kRing; ++s)
+        if (sm.last_issued[s] != kNone)
+            (void)cctdev::mbar_wait_bounded(&sm.full[s], (sm.last_issued[s] / kRing) & 1u, kTmaPolls);
+}
+
+// Dataflow: wait (thread 0 polls, wall-clock limit) until particle block `blk` has finished
+// `k` stages, i.e. its stage-k positions are written.  CTA-uniform verdict; false = stop.
+static __device__ bool flow_wait(const TrackParams &P, TrackSmem &sm, int64_t blk, int k) {
+    if (threadIdx.x == 0) {
+        volatile unsigned *ready = P.flow_ready + blk;
+        volatile int *err = reinterpret_cast<volatile int *>(P.ctrl + CW_ERR);
+        int ok = *err == CCT_ERR_TIMEOUT ? 0 : 1;
+        if (ok && (int)*ready < k) {
+            const unsigned long long t0 = global_ns();
+            unsigned polls = 0;
+            while ((int)*ready < k) {
+                if (*err == CCT_ERR_TIMEOUT) {
+                    ok = 0;
+                    break;
+                }
+                if ((++polls & 255u) == 0 && global_ns() - t0 > P.wait_ns) {
+                    set_timeout(P);
+                    ok = 0;
+                    break;
+                }
+                __nanosleep(64);
+            }
+        }
+        __threadfence();
+        sm.verdict = ok;
+    }
+    __syncthreads();
+    return sm.verdict != 0;
+}
+
+// Dataflow: the calling CTA has written the partial sums of one unit of block `blk` at stage
+// k; true (CTA-uniform) if it was the block's last unit of that stage (cd units per stage).
+static __device__ bool flow_complete(const TrackParams &P, TrackSmem &sm, int64_t blk, int k, int64_t cd) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        const unsigned long long prev = atomicAdd(P.flow_done + blk, 1ull);
+        const bool last = (long long)prev + 1 == (long long)(k + 1) * cd;
+        if (last) __threadfence();
+        sm.verdict = last;
+    }
+    __syncthreads();
+    return sm.verdict != 0;
 }
 
 // cross product with the reference's component formula (point.py:402-410), unfused
@@ -264,9 +345,9 @@ static __device__ __forceinline__ void unit_prefetch(const TrackParams &P, int64
 // claims the CTA's next unit of the phase and issues that unit's first tiles, so that their
 // copies overlap this unit's reduction.  Returns the next unit (>= n_units: none), or -1 if a
 // TMA wait gave up (CCT_ERR_TIMEOUT recorded).
-template <int PPT, bool GRAD>
+template <int PPT, bool GRAD, bool FLOW = false>
 static __device__ int64_t unit_sum_f32c(const TrackParams &P, const PointSrc &src, int64_t u, TrackSmem &sm,
-                                        uint32_t &kt, int phase, int64_t n_units) {
+                                        uint32_t &kt, int phase, int64_t n_units, int64_t n_seq = 0) {
     const UnitRef U = locate_unit(P, u);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int G = P.G;
@@ -317,18 +398,20 @@ static __device__ int64_t unit_sum_f32c(const TrackParams &P, const PointSrc &sr
     if (__syncthreads_or(!ok_all)) {
         if (tid == 0) {
             set_timeout(P);
-            // let the last copy into every slot land before shared memory is given up (earlier
-            // copies into a slot were consumed before its refill)
-            for (int s = 0; s < kRing; ++s)
-                if (sm.last_issued[s] != kNone)
-                    (void)cctdev::mbar_wait_bounded(&sm.full[s], (sm.last_issued[s] / kRing) & 1u, kTmaPolls);
+            ring_drain(sm);
         }
         __syncthreads();
         return -1;
     }
     kt += (uint32_t)nt;
-    const int64_t next = next_unit(P, sm, phase);   // all warps are past their last tile
-    if (next < n_units) unit_prefetch(P, next, sm, kt);
+    // all warps are past their last tile: claim the next unit and start its copies, so that
+    // they overlap this unit's reduction (FLOW: the caller claims after the unit is counted,
+    // so that a CTA that then runs a block update holds no claimed unit meanwhile)
+    int64_t next = 0;
+    if (!FLOW) {
+        next = next_unit(P, sm, phase);
+        if (next < n_units) unit_prefetch(P, next, sm, kt);
+    }
 
     // reduce the S slices of every particle in fixed order
 #pragma unroll
@@ -479,6 +562,68 @@ static __device__ void particle_update(const TrackParams &P, int64_t pi, int ste
     }
 }
 
+// Dataflow: the particle update of block (d, b) after its last unit of stage k, then the
+// block is marked ready for stage k + 1.  A thread takes up to kMaxGroup / kTrackBlock of the
+// block's particles at once and sums their chunk partials in chunk order (four accumulators
+// per particle, combined in a fixed pattern: deterministic); neighbouring threads read
+// neighbouring particles' partials, and each thread keeps 12 loads per particle in flight.
+static __device__ void block_update(const TrackParams &P, int d, int64_t b, int k) {
+    constexpr int R = kMaxGroup / kTrackBlock;   // particles per thread
+    const int step = P.step_begin + k / 4, stage = k % 4;
+    const int G = P.G;
+    const int64_t cd = P.chunks[d];
+    const int64_t stride = (int64_t)G * 3;       // doubles between a particle's chunk partials
+    const double *base = P.partial + (P.unit_off[d] + b * cd) * stride;
+    double a[R][4][3];
+#pragma unroll
+    for (int r = 0; r < R; ++r)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) a[r][q][0] = a[r][q][1] = a[r][q][2] = 0.0;
+    int64_t c = 0;
+    for (; c + 4 <= cd; c += 4) {
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            const int slot = threadIdx.x + r * kTrackBlock;
+            if (slot >= G) break;
+            double v[4][3];
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+#pragma unroll
+                for (int x = 0; x < 3; ++x) v[q][x] = base[(c + q) * stride + slot * 3 + x];
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+#pragma unroll
+                for (int x = 0; x < 3; ++x) a[r][q][x] += v[q][x];
+        }
+    }
+    for (; c < cd; ++c) {
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            const int slot = threadIdx.x + r * kTrackBlock;
+            if (slot >= G) break;
+#pragma unroll
+            for (int x = 0; x < 3; ++x) a[r][0][x] += base[c * stride + slot * 3 + x];
+        }
+    }
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        const int slot = threadIdx.x + r * kTrackBlock;
+        const int64_t j = b * G + slot;
+        if (slot >= G || j >= P.n_p) continue;
+        const int64_t pi = (int64_t)d * P.n_p + j;
+        if (!particle_active(P, pi, step)) continue;
+        double B[3];
+#pragma unroll
+        for (int x = 0; x < 3; ++x) B[x] = (a[r][0][x] + a[r][1][x]) + (a[r][2][x] + a[r][3][x]);
+        particle_update(P, pi, step, stage, B);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        atomicExch(P.flow_ready + (int64_t)d * P.blocks + b, (unsigned)(k + 1));
+    }
+}
+
 // ---------------------------------------------------------------- unit planner (host and device)
 __host__ __device__ inline int64_t hd_max(int64_t a, int64_t b) { return a > b ? a : b; }
 __host__ __device__ inline int64_t hd_min(int64_t a, int64_t b) { return a < b ? a : b; }
@@ -535,5 +680,6 @@ int64_t plan_units(const int64_t *hoff, int n_designs, int64_t n_p, int G, int g
                    int64_t *chunks, int64_t *chunk_tiles);
 int64_t units_bound(int n_designs, int64_t n_p, int G, int grid);
 cudaError_t launch_track_kernel(TrackParams &P, int grid, cudaStream_t st);
+void set_flow(TrackParams &P, unsigned char *flow);
 
 }  // namespace cctgpu
