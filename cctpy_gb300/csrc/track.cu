@@ -6,19 +6,28 @@
 //
 // Work decomposition.  Each design's particles are cut into blocks of G particles and its
 // segments into tiles of 128, the tiles into chunks.  A unit is (design, block, chunk).
-// Every RK4 stage runs two phases separated by grid barriers:
-//   A. each CTA takes units (u = blockIdx.x, += gridDim.x) and computes the chunk's field at
-//      the stage positions of the block's particles:
+// Every RK4 stage has two parts:
+//   A. field sums: a CTA takes a unit and computes the chunk's field at the stage positions
+//      of the block's particles, one partial per (unit, particle):
 //        FP32c: the chunk's packed tiles stream into a shared-memory ring by TMA bulk copies;
 //               every warp reads every tile; a warp owns 32*PPT particles and a 128/S-segment
-//               slice of each tile (S = 8 * 32 * PPT / G), lanes hold particles;
-//        FP64:  G = 32, the 8 warps split the chunk's tiles, lane = particle, segments are
+//               slice of each tile (S = 2 * 32 * PPT / G), lanes hold particles;
+//        FP64:  G = 32, the 2 warps split the chunk's tiles, lane = particle, segments are
 //               read with warp-uniform loads;
-//      the S slices are reduced in fixed order and one partial per (unit, particle) is stored;
-//   C. each thread takes particles, sums the chunk partials of its particle in fixed order,
-//      adds the analytic QS fields and advances the RK4 bookkeeping.
-// Grid barriers count on a global word and have a wall-clock limit after which the kernel
-// records CCT_ERR_TIMEOUT and returns; TMA waits are bounded too.  No wait is unbounded.
+//   C. particle update: the chunk partials of a particle are summed in fixed order, the
+//      analytic QS fields added and the RK4 bookkeeping advanced.
+// Two schedules:
+//   * dataflow (8 or more particle blocks): one sequence of units over all stages, handed
+//     out by a global counter.  Before a unit a CTA waits until the unit's block has finished
+//     the previous stage (per-block stage counter); after it, it counts the unit done on the
+//     block; the CTA that completes a block's stage runs part C for that block and marks it
+//     ready.  Blocks of different stages overlap, so no CTA waits at a stage's end.
+//   * grid barriers (fewer blocks): part A with units taken from a per-stage counter, a grid
+//     barrier, part C on every CTA at once (a warp per particle), a grid barrier; for a small
+//     batch part C is shortest this way.
+// Grid barriers and dataflow waits count on global words and have a wall-clock limit after
+// which the kernel records CCT_ERR_TIMEOUT and returns; TMA waits are bounded too.  No wait
+// is unbounded.
 #include <cstdlib>
 #include <mutex>
 #include <vector>

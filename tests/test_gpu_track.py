@@ -61,6 +61,27 @@ def test_design_population_one_launch(golden, prec, ptol, vtol):
         check(out[d], golden[f"dp{d}_particles_out"], ptol, vtol)
 
 
+@pytest.mark.parametrize("prec,ptol,vtol,same", [("f64", POS_TOL_F64, VEL_RTOL_F64, 1e-12),
+                                                 ("f32c", POS_TOL_F32C, 1e-6, 1e-8)])
+def test_dataflow_schedule_matches_reference_and_barrier_schedule(golden, prec, ptol, vtol, same):
+    """Eight copies of the gantry section in one launch are eight particle blocks, which the
+    kernel runs on its dataflow schedule (per-block stage counters); one copy alone runs on
+    grid barriers.  Every copy must give the reference's track.  Between the two launches the
+    segment chunks differ (the planner sizes them for the whole batch) as well as the order of
+    the chunk sums: FP64 tracks agree to 1e-12, FP32c ones to the FP32 rounding of a different
+    chunk split (1e-8 m)."""
+    bl = W.build_gantry_section()
+    parts = golden["gs_particles_in"]
+    one = engine.track(engine.design_of(bl), parts, 3.5, 0.05, prec)[0]
+    many = engine.track(engine.design_set_of([bl] * 8), np.stack([parts] * 8), 3.5, 0.05, prec)
+    for d in range(8):
+        check(many[d], golden["gs_particles_out"], ptol, vtol)
+        np.testing.assert_array_equal(many[d], many[0])     # same inputs, same chunks: same track
+        assert np.abs(many[d][:, 0:3] - one[:, 0:3]).max() < same
+        assert np.abs(many[d][:, 3:6] - one[:, 3:6]).max() / np.abs(one[:, 3:6]).max() < same
+        assert np.array_equal(many[d][:, 6:], one[:, 6:])
+
+
 def test_ragged_particle_counts_match_oracle(records_json):
     # 37 particles: one full group of 32 and a ragged group of 5; short track, oracle in seconds
     bl = HUST_SC_GANTRY().create_second_bending_part_beamline()
