@@ -588,7 +588,7 @@ static int launch_adjoint(const double *kls, const double *p0s, const int64_t *s
     P.barrier_blocks = (unsigned)(grid + g_test_phantom_blocks);
     P.wait_ns = (unsigned long long)g_wait_ms * 1000000ull;
     P.record = nullptr;
-    set_flow(P, sc + L.flow_off);   // the forward launches; the reverse sweep keeps its barriers
+    set_flow(P, sc + L.flow_off);   // the forward launches (the reverse sweep keeps its barriers)
 
     // 1. state from the records; learn the step count
     CCT_TRY_CUDA(cudaMemsetAsync(sc, 0, 256, st));
@@ -653,6 +653,11 @@ static int launch_adjoint(const double *kls, const double *p0s, const int64_t *s
         }
         A.T = P;
         A.T.barrier_blocks = (unsigned)(agrid + g_test_phantom_blocks);
+        // The reverse sweep stays on grid barriers.  Measured on the dataflow schedule it was
+        // slower: of the eight CTAs on an SM the warp scheduler favours some, the others' units
+        // run up to 20x longer while the SM is full, and on dataflow their blocks' late stages
+        // hold back the next stage; behind a barrier they only finish last.
+        A.T.use_flow = 0;
         A.step_begin = P.step_begin;
         A.step_end = P.step_end;
         void *args[] = {&A};

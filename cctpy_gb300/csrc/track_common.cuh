@@ -193,19 +193,24 @@ static __device__ bool flow_wait(const TrackParams &P, TrackSmem &sm, int64_t bl
         volatile int *err = reinterpret_cast<volatile int *>(P.ctrl + CW_ERR);
         int ok = *err == CCT_ERR_TIMEOUT ? 0 : 1;
         if (ok && (int)*ready < k) {
+            // back off (64 ns doubling to 4 us): many CTAs polling a few hot words would
+            // otherwise load the L2 slices that also serve the running units' tiles
             const unsigned long long t0 = global_ns();
-            unsigned polls = 0;
+            unsigned polls = 0, nap = 64;
             while ((int)*ready < k) {
-                if (*err == CCT_ERR_TIMEOUT) {
-                    ok = 0;
-                    break;
+                if ((++polls & 15u) == 0) {
+                    if (*err == CCT_ERR_TIMEOUT) {
+                        ok = 0;
+                        break;
+                    }
+                    if (global_ns() - t0 > P.wait_ns) {
+                        set_timeout(P);
+                        ok = 0;
+                        break;
+                    }
                 }
-                if ((++polls & 255u) == 0 && global_ns() - t0 > P.wait_ns) {
-                    set_timeout(P);
-                    ok = 0;
-                    break;
-                }
-                __nanosleep(64);
+                __nanosleep(nap);
+                if (nap < 4096) nap *= 2;
             }
         }
         __threadfence();
@@ -562,14 +567,15 @@ static __device__ void particle_update(const TrackParams &P, int64_t pi, int ste
     }
 }
 
-// Dataflow: the particle update of block (d, b) after its last unit of stage k, then the
-// block is marked ready for stage k + 1.  A thread takes up to kMaxGroup / kTrackBlock of the
-// block's particles at once and sums their chunk partials in chunk order (four accumulators
-// per particle, combined in a fixed pattern: deterministic); neighbouring threads read
-// neighbouring particles' partials, and each thread keeps 12 loads per particle in flight.
-static __device__ void block_update(const TrackParams &P, int d, int64_t b, int k) {
+// Dataflow: block (d, b) has finished stage k of its field sums.  Sums each of its particles'
+// chunk partials, calls fn(pi, B) for it (the thread that summed it), and marks the block
+// ready for stage k + 1.  A thread takes up to kMaxGroup / kTrackBlock particles at once and
+// sums their partials in chunk order (four accumulators per particle, combined in a fixed
+// pattern: deterministic); neighbouring threads read neighbouring particles' partials, and
+// each thread keeps 12 loads per particle in flight.
+template <typename Fn>
+static __device__ void block_finish(const TrackParams &P, int d, int64_t b, int k, Fn fn) {
     constexpr int R = kMaxGroup / kTrackBlock;   // particles per thread
-    const int step = P.step_begin + k / 4, stage = k % 4;
     const int G = P.G;
     const int64_t cd = P.chunks[d];
     const int64_t stride = (int64_t)G * 3;       // doubles between a particle's chunk partials
@@ -610,18 +616,24 @@ static __device__ void block_update(const TrackParams &P, int d, int64_t b, int 
         const int slot = threadIdx.x + r * kTrackBlock;
         const int64_t j = b * G + slot;
         if (slot >= G || j >= P.n_p) continue;
-        const int64_t pi = (int64_t)d * P.n_p + j;
-        if (!particle_active(P, pi, step)) continue;
         double B[3];
 #pragma unroll
         for (int x = 0; x < 3; ++x) B[x] = (a[r][0][x] + a[r][1][x]) + (a[r][2][x] + a[r][3][x]);
-        particle_update(P, pi, step, stage, B);
+        fn((int64_t)d * P.n_p + j, B);
     }
     __syncthreads();
     if (threadIdx.x == 0) {
         __threadfence();
         atomicExch(P.flow_ready + (int64_t)d * P.blocks + b, (unsigned)(k + 1));
     }
+}
+
+// Forward tracking: stage k of the launch is stage k % 4 of step step_begin + k / 4.
+static __device__ void block_update(const TrackParams &P, int d, int64_t b, int k) {
+    const int step = P.step_begin + k / 4, stage = k % 4;
+    block_finish(P, d, b, k, [&](int64_t pi, const double *B) {
+        if (particle_active(P, pi, step)) particle_update(P, pi, step, stage, B);
+    });
 }
 
 // ---------------------------------------------------------------- unit planner (host and device)
