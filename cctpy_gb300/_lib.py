@@ -45,6 +45,7 @@ SIGNATURES = {
     "cct_beam_readout": (ctypes.c_int, [_p, _i32, _i64, _p, _p, _i32, _i32, _p, _p, _p]),
     "cct_probe_fma_peak": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_double)]),
     "cct_test_set_barrier_fault": (ctypes.c_int, [ctypes.c_int, ctypes.c_int]),
+    "cct_test_set_flow_fault": (ctypes.c_int, [ctypes.c_int, ctypes.c_int]),
 }
 
 _lib = None

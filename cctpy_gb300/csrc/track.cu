@@ -156,6 +156,7 @@ cudaError_t launch_track_kernel(TrackParams &P, int grid, cudaStream_t st) {
 }
 
 int g_test_phantom_blocks = 0;
+int g_test_flow_skew = 0;
 long long g_wait_ms = 60000;
 
 TrackScratchLayout track_scratch_layout(int n_designs, int64_t n_particles, int64_t n_units, int group) {
@@ -199,6 +200,7 @@ int g_units_per_cta = kUnitsPerCta;
 void set_flow(TrackParams &P, unsigned char *flow) {
     P.blocks = (P.n_p + P.G - 1) / P.G;
     P.use_flow = (int64_t)P.n_designs * P.blocks >= kFlowMinBlocks ? 1 : 0;
+    P.flow_skew = g_test_flow_skew;
     P.flow_done = reinterpret_cast<unsigned long long *>(flow);
     P.flow_ready = reinterpret_cast<unsigned *>(flow + 8 * (int64_t)P.n_designs * P.blocks);
 }
@@ -463,6 +465,14 @@ int track_status(const void *scratch, cudaStream_t st) {
 }
 
 }  // namespace cctgpu
+
+extern "C" int cct_test_set_flow_fault(int stages_ahead, int wait_ms) {
+    // Test hook: dataflow waits require `stages_ahead` more finished stages than they need
+    // (so that they run out), and the wait limit is shortened.
+    cctgpu::g_test_flow_skew = stages_ahead < 0 ? 0 : stages_ahead;
+    cctgpu::g_wait_ms = wait_ms > 0 ? wait_ms : 60000;
+    return CCT_OK;
+}
 
 extern "C" int cct_test_set_barrier_fault(int phantom_blocks, int wait_ms) {
     // Test hook: count `phantom_blocks` CTAs that never arrive, and shorten the wait limit,

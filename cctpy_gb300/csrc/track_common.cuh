@@ -62,6 +62,7 @@ struct TrackParams {
     double *record;                // null, or per (step, stage, particle): stage state + field
     // dataflow schedule (use_flow = 1): per particle block (design d, block b at d * blocks + b)
     int use_flow;
+    int flow_skew;                 // test hook: extra stages every wait requires (0 in use)
     int64_t blocks;                // particle blocks per design
     unsigned long long *flow_done; // units finished, all stages of this launch
     unsigned *flow_ready;          // stages whose particle update is complete
@@ -192,6 +193,7 @@ static __device__ bool flow_wait(const TrackParams &P, TrackSmem &sm, int64_t bl
         volatile unsigned *ready = P.flow_ready + blk;
         volatile int *err = reinterpret_cast<volatile int *>(P.ctrl + CW_ERR);
         int ok = *err == CCT_ERR_TIMEOUT ? 0 : 1;
+        k += P.flow_skew;
         if (ok && (int)*ready < k) {
             // back off (64 ns doubling to 4 us): many CTAs polling a few hot words would
             // otherwise load the L2 slices that also serve the running units' tiles
@@ -685,6 +687,7 @@ __host__ __device__ inline int64_t plan_units_hd(const int64_t *seg_off, int n_d
 // ---------------------------------------------------------------- host helpers (track.cu)
 extern int g_units_per_cta;
 extern int g_test_phantom_blocks;
+extern int g_test_flow_skew;
 extern long long g_wait_ms;
 int group_size(int precision, int64_t n_p);
 int track_grid(int *grid_out);

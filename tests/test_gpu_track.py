@@ -139,6 +139,24 @@ def test_bounded_barrier_wait_reports_timeout(golden):
     assert np.isfinite(out).all()
 
 
+def test_bounded_dataflow_wait_reports_timeout(golden):
+    """Eight designs run on the dataflow schedule; a wait for a particle block that never
+    finishes its stage (the test hook asks one stage more than exists) gives up after the
+    wait limit and reports CCT_ERR_TIMEOUT; the context stays usable afterwards."""
+    _, cct = W.build_single_dipole()
+    ds = engine.design_set_of([cct] * 8)
+    parts = np.stack([golden["sd_particles_in"][:2]] * 8)
+    lib = _lib.load()
+    lib.cct_test_set_flow_fault(1, 300)
+    try:
+        with pytest.raises(_lib.CctTimeoutError):
+            engine.track(ds, parts, 0.01, 0.001, "f32c")
+    finally:
+        lib.cct_test_set_flow_fault(0, 0)
+    out = engine.track(ds, parts, 0.01, 0.001, "f32c")
+    assert np.isfinite(out).all()
+
+
 def test_nonfinite_particle_is_reported(golden):
     _, cct = W.build_single_dipole()
     ps = golden["sd_particles_in"][:3].copy()
