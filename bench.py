@@ -220,12 +220,17 @@ def measure_tracking(args, dev, rank):
         pp = W.beam_particles(bls[0], 512, seed=2 + rank, kinetic_MeV=215.0)
         tp = timed(dsp, pp, s32 // 2, "f32c", reps=1)
         rp = 64 * 512 * (s32 // 2) / tp
+        tp64 = timed(dsp, pp, 1, "f64", reps=1)
+        rp64 = 64 * 512 / tp64
         segs = [dsp.segments_of(d) for d in range(64)]
         out["design_population"] = {
             "workload": f"64 designs ({min(segs)}..{max(segs)} segments, {dsp.n_segments} total), 512 protons each, "
                         "one launch",
             "f32c": {"steps": s32 // 2, "seconds": tp, "particle_steps_per_s": rp,
                      "gpairs_per_s": 512 * (s32 // 2) * 4 * dsp.n_segments / tp / 1e9},
+            "f64": {"steps": 1, "seconds": tp64, "particle_steps_per_s": rp64,
+                    "gpairs_per_s": 512 * 4 * dsp.n_segments / tp64 / 1e9},
+            "speedup_f32c_vs_f64": rp / rp64,
             "f32c_autotuned": tuned(dsp, pp, s32 // 2, 512)}
     if not args.no_adjoint:
         out["design_gradients"] = measure_design_grads(args, rank)
