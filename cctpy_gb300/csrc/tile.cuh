@@ -235,7 +235,7 @@ namespace cctgpu {
 
 // Adjoint counterpart of tile_f32c: for PPT points with weights a (per point), accumulate
 // grad_p (a . B_i) = c |r|^-3 - 3 (c.r) r |r|^-5, c = a x kl_i, over segments [4*g0, 4*g1)
-// of one tile, with the same compensation (FP32 sub-blocks of <= 64 segments, Kahan (S, C)).
+// of one tile, with the same compensation (FP32 sums over 32-segment sub-blocks, Kahan (S, C)).
 template <int PPT, int JU = 1>
 __device__ __forceinline__ void tile_grad_f32c(const unsigned char *tile, const float (&ph)[PPT][3],
                                                const float (&pl)[PPT][3], const float (&a)[PPT][3],
@@ -254,14 +254,15 @@ __device__ __forceinline__ void tile_grad_f32c(const unsigned char *tile, const 
             NA[i][c] = f2_pack(-a[i][c], -a[i][c]);
         }
     const f2 m3 = f2_pack(-3.0f, -3.0f);
-    // g0 and g1 are multiples of 16 (sub-blocks of 64 segments)
+    constexpr int SG = kSub / 4;          // 4-segment groups per FP32 sub-sum
+    // g0 and g1 are multiples of SG (a slice of a tile holds whole sub-blocks)
 #pragma unroll 1
-    for (int sb = g0; sb < g1; sb += 16) {
+    for (int sb = g0; sb < g1; sb += SG) {
         f2 G[PPT][3];
 #pragma unroll
         for (int i = 0; i < PPT; ++i) G[i][0] = G[i][1] = G[i][2] = 0ull;
 #pragma unroll JU
-        for (int j = sb; j < sb + 16; ++j) {
+        for (int j = sb; j < sb + SG; ++j) {
             const ulonglong2 KX = v[0 * Q + j], KY = v[1 * Q + j], KZ = v[2 * Q + j];
             const ulonglong2 PX = v[6 * Q + j], PY = v[7 * Q + j], PZ = v[8 * Q + j];
 #pragma unroll

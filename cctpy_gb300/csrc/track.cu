@@ -11,9 +11,9 @@
 //      of the block's particles, one partial per (unit, particle):
 //        FP32c: the chunk's packed tiles stream into a shared-memory ring by TMA bulk copies;
 //               every warp reads every tile; a warp owns 32*PPT particles and a 128/S-segment
-//               slice of each tile (S = 2 * 32 * PPT / G), lanes hold particles;
-//        FP64:  G = 32, the 2 warps split the chunk's tiles, lane = particle, segments are
-//               read with warp-uniform loads;
+//               slice of each tile (S = warps * 32 * PPT / G), lanes hold particles;
+//        FP64:  G = 32, the CTA's warps split the chunk's tiles, lane = particle, segments
+//               are read with warp-uniform loads;
 //   C. particle update: the chunk partials of a particle are summed in fixed order, the
 //      analytic QS fields added and the RK4 bookkeeping advanced.
 // Two schedules:

@@ -9,8 +9,10 @@
 
 namespace cctgpu {
 
-constexpr int kTrackBlock = 64;      // 2 warps; 8 CTAs per SM, which take units dynamically
-constexpr int kTrackMinBlocks = 8;
+// 4 warps per CTA, 3 CTAs per SM (up to 168 registers a thread): measured faster than 8 CTAs
+// of 2 warps capped at 128 registers (gantry section 1890 -> 1950 Gpairs/s)
+constexpr int kTrackBlock = 128;
+constexpr int kTrackMinBlocks = 3;
 constexpr int kTrackWarps = kTrackBlock / 32;
 static_assert((kTile / kTrackWarps) % kSub == 0, "tile slices hold whole FP32c sub-blocks");
 constexpr int kMaxGroup = 64 * kTrackWarps;   // particles per unit: 2 per lane in every warp
