@@ -653,10 +653,10 @@ static int launch_adjoint(const double *kls, const double *p0s, const int64_t *s
         }
         A.T = P;
         A.T.barrier_blocks = (unsigned)(agrid + g_test_phantom_blocks);
-        // The reverse sweep stays on grid barriers.  Measured on the dataflow schedule it was
-        // slower: of the eight CTAs on an SM the warp scheduler favours some, the others' units
-        // run up to 20x longer while the SM is full, and on dataflow their blocks' late stages
-        // hold back the next stage; behind a barrier they only finish last.
+        // The reverse sweep stays on grid barriers: measured on the dataflow schedule it was
+        // no faster with 3 CTAs of 4 warps per SM, and slower with 8 CTAs of 2 warps (the warp
+        // scheduler favoured some CTAs of an SM, the others' units ran up to 20x longer, and
+        // their blocks' late stages held back the next stage).
         A.T.use_flow = 0;
         A.step_begin = P.step_begin;
         A.step_end = P.step_end;
