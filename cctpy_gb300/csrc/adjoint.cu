@@ -345,8 +345,9 @@ __global__ void __launch_bounds__(kSegBlock) seg_adjoint_kernel(TrackParams P, i
 // 30 FMA-pipe operations per pair instead of 35.  Each chunk's result is Kahan-added per
 // segment.
 constexpr int kSegPts = 128;
-constexpr int kSegThreads = 64;
+constexpr int kSegThreads = 32;     // one warp per tile, two packed segment pairs per thread
 constexpr int kSegUnroll = 4;
+constexpr int kSegMinBlocks = 8;   // CTAs per SM the register budget allows for (184 registers used)
 
 __global__ void seg_prep_kernel(const double *__restrict__ record, int64_t n_rec, float4 *__restrict__ out) {
     for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n_rec; e += (int64_t)gridDim.x * blockDim.x) {
@@ -359,11 +360,12 @@ __global__ void seg_prep_kernel(const double *__restrict__ record, int64_t n_rec
     }
 }
 
-__global__ void __launch_bounds__(kSegThreads, 8) seg_adjoint_f32c_kernel(TrackParams P, int n_steps,
+__global__ void __launch_bounds__(kSegThreads, kSegMinBlocks) seg_adjoint_f32c_kernel(TrackParams P, int n_steps,
                                                                           const float4 *__restrict__ pts_df,
                                                                           double *grad) {
     // per point, as packed pairs (v, v): a x3, q x3, n x3 with n = q x a, pad (80 B: five 16-byte loads)
     __shared__ __align__(16) f2 pts[kSegPts][10];
+    constexpr int R = kTile / 2 / kSegThreads;      // packed segment pairs per thread
     const int64_t t = blockIdx.x;
     int lo = 0, hi = P.n_designs - 1;               // design of tile t: last d with tile_off[d] <= t
     while (lo < hi) {
@@ -378,15 +380,25 @@ __global__ void __launch_bounds__(kSegThreads, 8) seg_adjoint_f32c_kernel(TrackP
     const int tid = threadIdx.x;
     const int cnt = h->count;
     const int64_t s0 = P.seg_off[d] + (t - P.tile_off[d]) * kTile;
-    const f2 kx = v[0 * Q2 + tid], ky = v[1 * Q2 + tid], kz = v[2 * Q2 + tid];
-    const f2 px = v[6 * Q2 + tid], py = v[7 * Q2 + tid], pz = v[8 * Q2 + tid];
-    // h = p x kl
-    const f2 hx = f2_fma(py, kz, f2_mul(f2_neg(pz), ky));
-    const f2 hy = f2_fma(pz, kx, f2_mul(f2_neg(px), kz));
-    const f2 hz = f2_fma(px, ky, f2_mul(f2_neg(py), kx));
-    float S[2][6], C[2][6];
+    // pair r of this thread: packed index tid + r * kSegThreads (segments 2 * that and + 1)
+    f2 kx[R], ky[R], kz[R], px[R], py[R], pz[R], hx[R], hy[R], hz[R];
 #pragma unroll
-    for (int m = 0; m < 2; ++m)
+    for (int r = 0; r < R; ++r) {
+        const int e = tid + r * kSegThreads;
+        kx[r] = v[0 * Q2 + e];
+        ky[r] = v[1 * Q2 + e];
+        kz[r] = v[2 * Q2 + e];
+        px[r] = v[6 * Q2 + e];
+        py[r] = v[7 * Q2 + e];
+        pz[r] = v[8 * Q2 + e];
+        // h = p x kl
+        hx[r] = f2_fma(py[r], kz[r], f2_mul(f2_neg(pz[r]), ky[r]));
+        hy[r] = f2_fma(pz[r], kx[r], f2_mul(f2_neg(px[r]), kz[r]));
+        hz[r] = f2_fma(px[r], ky[r], f2_mul(f2_neg(py[r]), kx[r]));
+    }
+    float S[2 * R][6], C[2 * R][6];
+#pragma unroll
+    for (int m = 0; m < 2 * R; ++m)
 #pragma unroll
         for (int c = 0; c < 6; ++c) S[m][c] = C[m][c] = 0.0f;
     const f2 m3 = f2_pack(-3.0f, -3.0f);
@@ -398,8 +410,8 @@ __global__ void __launch_bounds__(kSegThreads, 8) seg_adjoint_f32c_kernel(TrackP
             const int64_t e = base + k;
             float q[3] = {0.f, 0.f, 0.f}, a[3] = {0.f, 0.f, 0.f};
             if (e < n_pts) {
-                const float4 *r = pts_df + 3 * ((e / P.n_p) * total + (int64_t)d * P.n_p + e % P.n_p);
-                const float4 u = r[0], w = r[1], z = r[2];
+                const float4 *rp = pts_df + 3 * ((e / P.n_p) * total + (int64_t)d * P.n_p + e % P.n_p);
+                const float4 u = rp[0], w = rp[1], z = rp[2];
                 q[0] = __fadd_rn(__fsub_rn(u.x, h->o_hi[0]), __fsub_rn(w.x, h->o_lo[0]));
                 q[1] = __fadd_rn(__fsub_rn(u.y, h->o_hi[1]), __fsub_rn(w.y, h->o_lo[1]));
                 q[2] = __fadd_rn(__fsub_rn(u.z, h->o_hi[2]), __fsub_rn(w.z, h->o_lo[2]));
@@ -423,7 +435,13 @@ __global__ void __launch_bounds__(kSegThreads, 8) seg_adjoint_f32c_kernel(TrackP
             pts[k][9] = 0ull;
         }
         __syncthreads();
-        f2 V[3] = {0ull, 0ull, 0ull}, W[3] = {0ull, 0ull, 0ull}, U[3] = {0ull, 0ull, 0ull}, T = 0ull;
+        f2 V[R][3], W[R][3], U[R][3], T[R];
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            T[r] = 0ull;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) V[r][c] = W[r][c] = U[r][c] = 0ull;
+        }
         const int np = (int)min((int64_t)kSegPts, n_pts - base);
 #pragma unroll kSegUnroll
         for (int i = 0; i < np; ++i) {
@@ -432,64 +450,74 @@ __global__ void __launch_bounds__(kSegThreads, 8) seg_adjoint_f32c_kernel(TrackP
             const f2 Ax = v0.x, Ay = v0.y, Az = v1.x;
             const f2 Qx = v1.y, Qy = v2.x, Qz = v2.y;
             const f2 Nx = v3.x, Ny = v3.y, Nz = v4.x;
-            const f2 rx = f2_sub(Qx, px), ry = f2_sub(Qy, py), rz = f2_sub(Qz, pz);
-            const f2 r2 = f2_fma(rx, rx, f2_fma(ry, ry, f2_mul(rz, rz)));
-            float l0, l1;
-            f2_unpack(r2, l0, l1);
-            const f2 inv = f2_pack(rsqrt_mufu(l0), rsqrt_mufu(l1));
-            const f2 inv2 = f2_mul(inv, inv);
-            const f2 inv3 = f2_mul(inv2, inv);
-            const f2 m3inv5 = f2_mul(f2_mul(inv3, inv2), m3);
-            V[0] = f2_fma(Nx, inv3, V[0]);
-            V[1] = f2_fma(Ny, inv3, V[1]);
-            V[2] = f2_fma(Nz, inv3, V[2]);
-            W[0] = f2_fma(Ax, inv3, W[0]);
-            W[1] = f2_fma(Ay, inv3, W[1]);
-            W[2] = f2_fma(Az, inv3, W[2]);
-            // kl.n + a.h = (a x kl).r
-            const f2 cr = f2_fma(kx, Nx, f2_fma(ky, Ny, f2_fma(kz, Nz, f2_fma(hx, Ax, f2_fma(hy, Ay, f2_mul(hz, Az))))));
-            const f2 tt = f2_mul(cr, m3inv5);
-            U[0] = f2_fma(tt, Qx, U[0]);
-            U[1] = f2_fma(tt, Qy, U[1]);
-            U[2] = f2_fma(tt, Qz, U[2]);
-            T = f2_add(T, tt);
+#pragma unroll
+            for (int r = 0; r < R; ++r) {
+                const f2 rx = f2_sub(Qx, px[r]), ry = f2_sub(Qy, py[r]), rz = f2_sub(Qz, pz[r]);
+                const f2 r2 = f2_fma(rx, rx, f2_fma(ry, ry, f2_mul(rz, rz)));
+                float l0, l1;
+                f2_unpack(r2, l0, l1);
+                const f2 inv = f2_pack(rsqrt_mufu(l0), rsqrt_mufu(l1));
+                const f2 inv2 = f2_mul(inv, inv);
+                const f2 inv3 = f2_mul(inv2, inv);
+                const f2 m3inv5 = f2_mul(f2_mul(inv3, inv2), m3);
+                V[r][0] = f2_fma(Nx, inv3, V[r][0]);
+                V[r][1] = f2_fma(Ny, inv3, V[r][1]);
+                V[r][2] = f2_fma(Nz, inv3, V[r][2]);
+                W[r][0] = f2_fma(Ax, inv3, W[r][0]);
+                W[r][1] = f2_fma(Ay, inv3, W[r][1]);
+                W[r][2] = f2_fma(Az, inv3, W[r][2]);
+                // kl.n + a.h = (a x kl).r
+                const f2 cr = f2_fma(kx[r], Nx, f2_fma(ky[r], Ny, f2_fma(kz[r], Nz,
+                              f2_fma(hx[r], Ax, f2_fma(hy[r], Ay, f2_mul(hz[r], Az))))));
+                const f2 tt = f2_mul(cr, m3inv5);
+                U[r][0] = f2_fma(tt, Qx, U[r][0]);
+                U[r][1] = f2_fma(tt, Qy, U[r][1]);
+                U[r][2] = f2_fma(tt, Qz, U[r][2]);
+                T[r] = f2_add(T[r], tt);
+            }
         }
         // per segment: dJ/dkl = V - p x W, grad_p = W x kl + U - p T
-        float v_[3][2], w_[3][2], u_[3][2], t_[2], p_[3][2], k_[3][2];
 #pragma unroll
-        for (int c = 0; c < 3; ++c) {
-            f2_unpack(V[c], v_[c][0], v_[c][1]);
-            f2_unpack(W[c], w_[c][0], w_[c][1]);
-            f2_unpack(U[c], u_[c][0], u_[c][1]);
-        }
-        f2_unpack(T, t_[0], t_[1]);
-        f2_unpack(px, p_[0][0], p_[0][1]);
-        f2_unpack(py, p_[1][0], p_[1][1]);
-        f2_unpack(pz, p_[2][0], p_[2][1]);
-        f2_unpack(kx, k_[0][0], k_[0][1]);
-        f2_unpack(ky, k_[1][0], k_[1][1]);
-        f2_unpack(kz, k_[2][0], k_[2][1]);
-#pragma unroll
-        for (int m = 0; m < 2; ++m) {
+        for (int r = 0; r < R; ++r) {
+            float v_[3][2], w_[3][2], u_[3][2], t_[2], p_[3][2], k_[3][2];
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
-                const int c1 = (c + 1) % 3, c2 = (c + 2) % 3;
-                const float dk = v_[c][m] - __fmaf_rn(p_[c1][m], w_[c2][m], -p_[c2][m] * w_[c1][m]);
-                const float gp = __fmaf_rn(w_[c1][m], k_[c2][m], -w_[c2][m] * k_[c1][m]) +
-                                 __fmaf_rn(-p_[c][m], t_[m], u_[c][m]);
-                kahan_add(S[m][c], C[m][c], dk);
-                kahan_add(S[m][3 + c], C[m][3 + c], gp);
+                f2_unpack(V[r][c], v_[c][0], v_[c][1]);
+                f2_unpack(W[r][c], w_[c][0], w_[c][1]);
+                f2_unpack(U[r][c], u_[c][0], u_[c][1]);
+            }
+            f2_unpack(T[r], t_[0], t_[1]);
+            f2_unpack(px[r], p_[0][0], p_[0][1]);
+            f2_unpack(py[r], p_[1][0], p_[1][1]);
+            f2_unpack(pz[r], p_[2][0], p_[2][1]);
+            f2_unpack(kx[r], k_[0][0], k_[0][1]);
+            f2_unpack(ky[r], k_[1][0], k_[1][1]);
+            f2_unpack(kz[r], k_[2][0], k_[2][1]);
+#pragma unroll
+            for (int m = 0; m < 2; ++m) {
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    const int c1 = (c + 1) % 3, c2 = (c + 2) % 3;
+                    const float dk = v_[c][m] - __fmaf_rn(p_[c1][m], w_[c2][m], -p_[c2][m] * w_[c1][m]);
+                    const float gp = __fmaf_rn(w_[c1][m], k_[c2][m], -w_[c2][m] * k_[c1][m]) +
+                                     __fmaf_rn(-p_[c][m], t_[m], u_[c][m]);
+                    kahan_add(S[2 * r + m][c], C[2 * r + m][c], dk);
+                    kahan_add(S[2 * r + m][3 + c], C[2 * r + m][3 + c], gp);
+                }
             }
         }
     }
 #pragma unroll
-    for (int m = 0; m < 2; ++m) {
-        const int j = 2 * tid + m;
-        if (j >= cnt) continue;
-        double *g = grad + 6 * (s0 + j);
-        for (int c = 0; c < 3; ++c) g[c] += (double)S[m][c] - (double)C[m][c];
-        for (int c = 0; c < 3; ++c) g[3 + c] -= (double)S[m][3 + c] - (double)C[m][3 + c];   // dJ/dp0 = -grad_p
-    }
+    for (int r = 0; r < R; ++r)
+#pragma unroll
+        for (int m = 0; m < 2; ++m) {
+            const int j = 2 * (tid + r * kSegThreads) + m;
+            if (j >= cnt) continue;
+            double *g = grad + 6 * (s0 + j);
+            for (int c = 0; c < 3; ++c) g[c] += (double)S[2 * r + m][c] - (double)C[2 * r + m][c];
+            for (int c = 0; c < 3; ++c)   // dJ/dp0 = -grad_p
+                g[3 + c] -= (double)S[2 * r + m][3 + c] - (double)C[2 * r + m][3 + c];
+        }
 }
 
 // ---------------------------------------------------------------- host side
