@@ -335,14 +335,15 @@ __global__ void __launch_bounds__(kSegBlock) seg_adjoint_kernel(TrackParams P, i
 // FP32c segment gradient.  seg_prep_kernel converts every recorded stage point once: its
 // position as a double-float pair (hi, lo) and its weight a in FP32, three float4 per point
 // {hx, hy, hz, ax}, {lx, ly, lz, ay}, {az, 0, 0, 0}.  seg_adjoint_f32c_kernel then runs one
-// 64-thread CTA per packed tile, two segments per thread (one packed pair); the design's
+// warp per packed tile, four segments per thread (two packed pairs, whose chains interleave
+// and share each staged point's loads); the design's
 // points are staged in shared memory 128 at a time in the tile's local frame (point minus
 // tile origin in double-float FP32, no FP64 work per tile) together with n = q x a, and the
 // sums are taken in moment form: with r = q - p,
 //   dJ/dkl  = sum (r x a) |r|^-3            = V - p x W,
 //   grad_p  = sum (a x kl) |r|^-3 + t r     = W x kl + U - p T,
 //   V = sum n |r|^-3, W = sum a |r|^-3, t = -3 (kl.n + a.(p x kl)) |r|^-5, U = sum t q, T = sum t,
-// 30 FMA-pipe operations per pair instead of 35.  Each chunk's result is Kahan-added per
+// 27 FMA-pipe operations per pair instead of 35.  Each chunk's result is Kahan-added per
 // segment.
 constexpr int kSegPts = 128;
 constexpr int kSegThreads = 32;     // one warp per tile, two packed segment pairs per thread
