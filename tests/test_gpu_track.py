@@ -139,6 +139,21 @@ def test_bounded_barrier_wait_reports_timeout(golden):
     assert np.isfinite(out).all()
 
 
+@pytest.mark.parametrize("prec,same", [("f64", 1e-12), ("f32c", 1e-8)])
+def test_dataflow_ragged_blocks_match_single_design_launches(prec, same):
+    """Five designs x 100 protons are ten particle blocks of 64 and 36 (dataflow schedule,
+    ragged blocks); each design tracked alone is two blocks (grid barriers)."""
+    _, cct = W.build_single_dipole()
+    parts = W.single_dipole_particles(100, seed=11)
+    many = engine.track(engine.design_set_of([cct] * 5), np.stack([parts] * 5), 0.05, 0.001, prec)
+    one = engine.track(engine.design_of(cct), parts, 0.05, 0.001, prec)[0]
+    for d in range(5):
+        np.testing.assert_array_equal(many[d], many[0])
+        assert np.abs(many[d][:, 0:3] - one[:, 0:3]).max() < same
+        assert np.abs(many[d][:, 3:6] - one[:, 3:6]).max() / np.abs(one[:, 3:6]).max() < same
+        assert np.array_equal(many[d][:, 6:], one[:, 6:])
+
+
 def test_bounded_dataflow_wait_reports_timeout(golden):
     """Eight designs run on the dataflow schedule; a wait for a particle block that never
     finishes its stage (the test hook asks one stage more than exists) gives up after the
