@@ -270,7 +270,11 @@ __device__ __forceinline__ UnitRef locate_unit(const TrackParams &P, int64_t u) 
     return r;
 }
 
-// Phase A, FP64: G = 32, warps split the chunk's tiles, lane = particle.
+// Phase A, FP64: G = 32, warps split the chunk's tiles, lane = particle.  A warp takes a
+// tile's segments 32 at a time: lane l loads segment l of the group and forms its moment
+// m = kl x (p0 - o) about the tile's first midpoint o, then the group's segments are broadcast
+// lane to lane and every lane sums A = sum kl |r|^-3, M = sum m |r|^-3 for its particle; the
+// tile's field is A x (p - o) - M (the moment form of the field kernel, in FP64).
 static __device__ void unit_field_f64(const TrackParams &P, int64_t u, TrackSmem &sm) {
     const UnitRef U = locate_unit(P, u);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -282,20 +286,43 @@ static __device__ void unit_field_f64(const TrackParams &P, int64_t u, TrackSmem
     const int64_t s_beg = P.seg_off[U.d], s_end = P.seg_off[U.d + 1];
     for (int64_t t = U.t_beg + warp; t < U.t_end; t += kTrackWarps) {
         const int64_t a = s_beg + t * kTile, e = min(s_end, a + kTile);
-        double tx = 0.0, ty = 0.0, tz = 0.0;
-        for (int64_t s = a; s < e; ++s) {
-            const double kx = __ldg(P.kls + 3 * s), ky = __ldg(P.kls + 3 * s + 1), kz = __ldg(P.kls + 3 * s + 2);
-            const double rx = px - __ldg(P.p0s + 3 * s), ry = py - __ldg(P.p0s + 3 * s + 1),
-                         rz = pz - __ldg(P.p0s + 3 * s + 2);
-            const double inv = rsqrt(rx * rx + ry * ry + rz * rz);
-            const double inv3 = inv * inv * inv;
-            tx += (ky * rz - kz * ry) * inv3;
-            ty += (kz * rx - kx * rz) * inv3;
-            tz += (kx * ry - ky * rx) * inv3;
+        const double ox = __ldg(P.p0s + 3 * a), oy = __ldg(P.p0s + 3 * a + 1), oz = __ldg(P.p0s + 3 * a + 2);
+        const double wx = px - ox, wy = py - oy, wz = pz - oz;
+        double Ax = 0.0, Ay = 0.0, Az = 0.0, Mx = 0.0, My = 0.0, Mz = 0.0;
+        for (int64_t g = a; g < e; g += 32) {
+            const int64_t s = g + lane;
+            double kx = 0.0, ky = 0.0, kz = 0.0, qx = 1.0e18, qy = 1.0e18, qz = 1.0e18;
+            if (s < e) {
+                kx = __ldg(P.kls + 3 * s);
+                ky = __ldg(P.kls + 3 * s + 1);
+                kz = __ldg(P.kls + 3 * s + 2);
+                qx = __ldg(P.p0s + 3 * s) - ox;
+                qy = __ldg(P.p0s + 3 * s + 1) - oy;
+                qz = __ldg(P.p0s + 3 * s + 2) - oz;
+            }
+            const double mx = ky * qz - kz * qy, my = kz * qx - kx * qz, mz = kx * qy - ky * qx;
+            const int n = (int)min((int64_t)32, e - g);
+            for (int k = 0; k < n; ++k) {
+                const double skx = __shfl_sync(0xffffffffu, kx, k), sky = __shfl_sync(0xffffffffu, ky, k),
+                             skz = __shfl_sync(0xffffffffu, kz, k);
+                const double sqx = __shfl_sync(0xffffffffu, qx, k), sqy = __shfl_sync(0xffffffffu, qy, k),
+                             sqz = __shfl_sync(0xffffffffu, qz, k);
+                const double smx = __shfl_sync(0xffffffffu, mx, k), smy = __shfl_sync(0xffffffffu, my, k),
+                             smz = __shfl_sync(0xffffffffu, mz, k);
+                const double rx = wx - sqx, ry = wy - sqy, rz = wz - sqz;
+                const double inv = rsqrt(rx * rx + ry * ry + rz * rz);
+                const double inv3 = inv * inv * inv;
+                Ax += skx * inv3;
+                Ay += sky * inv3;
+                Az += skz * inv3;
+                Mx += smx * inv3;
+                My += smy * inv3;
+                Mz += smz * inv3;
+            }
         }
-        bx += tx;
-        by += ty;
-        bz += tz;
+        bx += (Ay * wz - Az * wy) - Mx;
+        by += (Az * wx - Ax * wz) - My;
+        bz += (Ax * wy - Ay * wx) - Mz;
     }
     double *red = sm.red + (warp * 32 + lane) * 3;
     red[0] = bx;
