@@ -131,11 +131,20 @@ __global__ void __launch_bounds__(kTrackBlock, kTrackMinBlocks) track_kernel(Tra
             }
             if (!grid_barrier(P, sm)) return;   // a TMA timeout is recorded in CW_ERR and ends here
             reset_next_unit(P, phase);
-            for (int64_t pi = gwarp; pi < total; pi += nwarps) {   // a warp per particle
-                if (!particle_active(P, pi, step)) continue;
-                double B[3];
-                warp_sum_partials(P, pi, B);
-                if ((threadIdx.x & 31) == 0) particle_update(P, pi, step, stage, B);
+            if (total <= (int64_t)gridDim.x) {   // few particles: a CTA per particle
+                for (int64_t pi = blockIdx.x; pi < total; pi += gridDim.x) {
+                    if (!particle_active(P, pi, step)) continue;
+                    double B[3];
+                    cta_sum_partials(P, pi, B, sm);
+                    if (threadIdx.x == 0) particle_update(P, pi, step, stage, B);
+                }
+            } else {
+                for (int64_t pi = gwarp; pi < total; pi += nwarps) {   // a warp per particle
+                    if (!particle_active(P, pi, step)) continue;
+                    double B[3];
+                    warp_sum_partials(P, pi, B);
+                    if ((threadIdx.x & 31) == 0) particle_update(P, pi, step, stage, B);
+                }
             }
             if (!grid_barrier(P, sm)) return;
         }

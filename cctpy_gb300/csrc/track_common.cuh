@@ -536,6 +536,58 @@ static __device__ __forceinline__ void warp_sum_partials(const TrackParams &P, i
     out[2] = z;
 }
 
+// The same sum by the whole CTA (for batches with no more particles than CTAs, where the
+// particle update is the latency of the stage): thread t adds chunks t, t + blockDim, ... into
+// four accumulators in a fixed pattern, then a fixed-order tree in shared memory; all threads
+// get the total.
+static __device__ void cta_sum_partials(const TrackParams &P, int64_t pi, double out[3], TrackSmem &sm) {
+    const int tid = threadIdx.x;
+    const int d = (int)(pi / P.n_p);
+    const int64_t j = pi % P.n_p;
+    const int64_t b = j / P.G, slot = j % P.G;
+    const int64_t cd = P.chunks[d];
+    const int64_t u0 = P.unit_off[d] + b * cd;
+    double a[4][3] = {{0.0, 0.0, 0.0}, {0.0, 0.0, 0.0}, {0.0, 0.0, 0.0}, {0.0, 0.0, 0.0}};
+    int64_t c = tid;
+    for (; c + 3 * kTrackBlock < cd; c += 4 * kTrackBlock) {
+        double v[4][3];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const double *p = P.partial + ((u0 + c + k * kTrackBlock) * P.G + slot) * 3;
+            v[k][0] = p[0];
+            v[k][1] = p[1];
+            v[k][2] = p[2];
+        }
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+#pragma unroll
+            for (int q = 0; q < 3; ++q) a[k][q] += v[k][q];
+    }
+    for (; c < cd; c += kTrackBlock) {
+        const double *p = P.partial + ((u0 + c) * P.G + slot) * 3;
+        a[0][0] += p[0];
+        a[0][1] += p[1];
+        a[0][2] += p[2];
+    }
+    double *red = sm.red;   // kRedDoubles >= 3 * kTrackBlock
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < 3; ++q) red[3 * tid + q] = (a[0][q] + a[1][q]) + (a[2][q] + a[3][q]);
+    __syncthreads();
+    for (int w = kTrackBlock / 2; w > 0; w >>= 1) {
+        if (tid < w) {
+#pragma unroll
+            for (int q = 0; q < 3; ++q) red[3 * tid + q] += red[3 * (tid + w) + q];
+        }
+        __syncthreads();
+    }
+    out[0] = red[0];
+    out[1] = red[1];
+    out[2] = red[2];
+    __syncthreads();
+}
+static_assert(kRedDoubles >= 3 * kTrackBlock, "CTA partial-sum buffer");
+
 // True while particle pi still has RK4 steps at `step`.
 __device__ __forceinline__ bool particle_active(const TrackParams &P, int64_t pi, int step) {
     return (double)step < P.state[pi * kStateD + ST_NSTEPS];
