@@ -97,7 +97,8 @@ __global__ void __launch_bounds__(kTrackBlock, kTrackMinBlocks) track_kernel(Tra
         const double t_end = P.distance / speed;
         const double steps = ceil(t_end / dt0);
         S[ST_KQ] = r[7] / r[6];
-        const bool ok = isfinite(steps) && steps >= 1.0 && steps < 1.0e9;
+        // at most 5e8 steps, so that 4 stages a step stay within the int stage counters
+        const bool ok = isfinite(steps) && steps >= 1.0 && steps < 5.0e8;
         S[ST_NSTEPS] = ok ? steps : 0.0;
         S[ST_DT] = ok ? t_end / steps : 0.0;
         if (!ok) atomicExch(P.ctrl + CW_NONFINITE, 1u);

@@ -112,13 +112,16 @@ int cct_field_host(const double *h_kls, const double *h_p0s, int64_t n_seg,
  * distance += `distance`.
  *
  * One cooperative persistent launch; CTAs take (design, particle block,
- * segment chunk) units from a per-stage counter and meet at bounded grid
- * barriers between RK4 stages.  Needs caller-provided device scratch of
+ * segment chunk) units from a work counter.  With 8 or more particle blocks
+ * each block advances stage by stage as soon as its own units are done
+ * (bounded waits on per-block counters); smaller batches meet at bounded
+ * grid barriers between RK4 stages.  Needs caller-provided device scratch of
  * cct_track_scratch_bytes() bytes (256-byte aligned); a smaller buffer is
  * accepted down to the particle state plus one chunk per (design, particle
  * block), the work then being cut into fewer, larger units.  Returns
- * CCT_ERR_TIMEOUT if a barrier wait gives up and CCT_ERR_NONFINITE if a
- * particle state became non-finite (those particles are still written).
+ * CCT_ERR_TIMEOUT if a wait gives up and CCT_ERR_NONFINITE if a particle
+ * state became non-finite or needs 5e8 or more steps (those particles are
+ * still written).
  * Synchronous (reads the device status word before returning).
  * precision: 0 = FP64 (d_kls/d_p0s used), 1 = FP32-compensated (d_packed
  * used, built by cct_f32c_pack with the same design offsets).
