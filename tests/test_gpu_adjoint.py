@@ -150,7 +150,7 @@ def test_f32c_adjoint_matches_f64_adjoint_and_differences():
                      + [kw["dicct345_current"], kw["dicct345_current"], kw["agcct345_current"],
                         kw["agcct345_current"], 0.95])
     base = GantryDesign(theta, part_per_winding=60)
-    ps = W.beam_particles(base.beamline, 96, seed=7, kinetic_MeV=215.0)   # 96: blocks of 64, a ragged one
+    ps = W.beam_particles(base.beamline, 96, seed=7, kinetic_MeV=215.0)   # 96: a ragged block of 128
     L, step = 0.3, 0.01
     J64, g64 = design_gradients([base], ps, L, step, 215.0, checkpoint=8, precision="f64")
     J32, g32 = design_gradients([base], ps, L, step, 215.0, checkpoint=8, precision="f32c")

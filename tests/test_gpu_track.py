@@ -141,13 +141,14 @@ def test_bounded_barrier_wait_reports_timeout(golden):
 
 @pytest.mark.parametrize("prec,same", [("f64", 1e-12), ("f32c", 1e-8)])
 def test_dataflow_ragged_blocks_match_single_design_launches(prec, same):
-    """Five designs x 100 protons are ten particle blocks of 64 and 36 (dataflow schedule,
-    ragged blocks); each design tracked alone is two blocks (grid barriers)."""
+    """Nine designs x 100 protons: nine ragged particle blocks of 128 (FP32c) or 36 blocks of 32
+    (FP64, the last of each design ragged), run on the dataflow schedule; each design tracked
+    alone is one (FP32c) or four (FP64) blocks, on grid barriers."""
     _, cct = W.build_single_dipole()
     parts = W.single_dipole_particles(100, seed=11)
-    many = engine.track(engine.design_set_of([cct] * 5), np.stack([parts] * 5), 0.05, 0.001, prec)
+    many = engine.track(engine.design_set_of([cct] * 9), np.stack([parts] * 9), 0.05, 0.001, prec)
     one = engine.track(engine.design_of(cct), parts, 0.05, 0.001, prec)[0]
-    for d in range(5):
+    for d in range(9):
         np.testing.assert_array_equal(many[d], many[0])
         assert np.abs(many[d][:, 0:3] - one[:, 0:3]).max() < same
         assert np.abs(many[d][:, 3:6] - one[:, 3:6]).max() / np.abs(one[:, 3:6]).max() < same
