@@ -232,10 +232,71 @@ def measure_tracking(args, dev, rank):
                     "gpairs_per_s": 512 * 4 * dsp.n_segments / tp64 / 1e9},
             "speedup_f32c_vs_f64": rp / rp64,
             "f32c_autotuned": tuned(dsp, pp, s32 // 2, 512)}
+    out["reference_speed_test"] = measure_speed_test(rank)
     if not args.no_adjoint:
         out["design_gradients"] = measure_design_grads(args, rank)
     if not args.no_generation:
         out["optimiser_generation"] = measure_generation(args, rank)
+    return out
+
+
+def measure_speed_test(rank):
+    """The reference's own GPU speed test (final_code/work/小论文2回复/CPU和CPU代码速度测试.py:36-198):
+    100 copies of a 24 000-segment AG-CCT beamline (5 m drift, AG-CCT, 2 m drift, QS, 2 m drift;
+    10.8727 m), 16 copies of the ideal 250 MeV proton each, tracked over the whole length at its
+    20 mm and 2 mm steps, FP32c.  The reference reports 20 s and 68.39 s for this with 100
+    blocks x 1024 threads in FP32 (its hardware unstated; including its per-call kernel
+    compilation and host packing).  Timed here: the tracking call (host particle records in and
+    out), and the same with the design set built (host segments, upload, FP32c packing)."""
+    import torch
+    from cctpy_gb300 import Beamline, MM, ParticleFactory, engine
+    from cctpy_gb300.geometry import P2
+    from cctpy_gb300.particles import particles_to_array
+
+    def beamline():
+        return (Beamline.set_start_point(P2.origin()).first_drift(direct=P2.x_direct(), length=5)
+                .append_agcct(big_r=1.0, small_rs=[200 * MM, 180 * MM, 160 * MM, 140 * MM],
+                              bending_angles=[10, 10, 15, 15], tilt_angles=[[30], [90, 30]],
+                              winding_numbers=[[50], [10, 10, 15, 15]], currents=[10000, 10000])
+                .append_drift(2).append_qs(length=1, gradient=0, second_gradient=0, aperture_radius=200 * MM)
+                .append_drift(2))
+
+    bl = beamline()
+    L = bl.get_length()
+    ps = particles_to_array([ParticleFactory.create_proton_along(bl)] * 16)
+    warm = engine.design_set_of([bl] * 100)
+    engine.track(warm, ps, 0.04, 0.02, "f32c")
+    torch.cuda.synchronize()
+    out = {"workload": f"100 designs x {warm.segments_of(0)} segments (AG-CCT beamline, {L:.4f} m), 16 protons "
+                       "each, whole length, FP32c (the reference's GPU speed test)"}
+    for step, published in ((0.02, 20.0), (0.002, 68.39)):
+        n_steps = int(np.ceil(L / step))
+        pairs = 100 * 16 * n_steps * 4 * warm.segments_of(0)
+        t0 = time.perf_counter()
+        engine.track(warm, ps, L, step, "f32c")
+        torch.cuda.synchronize()
+        t_track = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        ds = engine.design_set_of([beamline() for _ in range(100)])
+        ds.packed()
+        engine.track(ds, ps, L, step, "f32c")
+        torch.cuda.synchronize()
+        t_all = time.perf_counter() - t0
+        out[f"step_{int(round(step * 1000))}mm"] = {
+            "steps": n_steps, "seconds": t_track, "gpairs_per_s": pairs / t_track / 1e9,
+            "seconds_with_design_set": t_all, "reference_published_seconds": published,
+            "reference_published_over_ours": published / t_all}
+    best = engine.autotune(warm, ps, 0.02, "f32c", steps=8)
+    try:
+        n_steps = int(np.ceil(L / 0.02))
+        t0 = time.perf_counter()
+        engine.track(warm, ps, L, 0.02, "f32c")
+        torch.cuda.synchronize()
+        t = time.perf_counter() - t0
+    finally:
+        engine.set_units_per_cta(0)
+    out["step_20mm"]["autotuned"] = {"units_per_cta": best, "seconds": t,
+                                     "gpairs_per_s": 100 * 16 * n_steps * 4 * warm.segments_of(0) / t / 1e9}
     return out
 
 

@@ -225,7 +225,7 @@ void set_flow(TrackParams &P, unsigned char *flow) {
 
 int64_t plan_units(const int64_t *hoff, int n_designs, int64_t n_p, int G, int grid, int64_t max_units,
                    int64_t *unit_off, int64_t *chunks, int64_t *chunk_tiles) {
-    return plan_units_hd(hoff, n_designs, n_p, G, (int64_t)g_units_per_cta * grid, max_units, unit_off, chunks,
+    return plan_units_hd(hoff, n_designs, n_p, G, (int64_t)g_units_per_cta * grid, grid, max_units, unit_off, chunks,
                          chunk_tiles);
 }
 
@@ -362,7 +362,8 @@ int launch_track(const double *kls, const double *p0s, const int64_t *seg_off, c
 // graph.  A one-thread kernel checks the offsets (and the packed set) and plans the units
 // on the device; the tracking kernel is launched cooperatively through cudaLaunchKernelEx;
 // the status stays in the scratch's control words for cct_track_status.
-__global__ void plan_kernel(TrackParams P, const unsigned char *packed, int64_t target_units, int64_t max_units,
+__global__ void plan_kernel(TrackParams P, const unsigned char *packed, int64_t target_units, int64_t min_units,
+                            int64_t max_units,
                             int64_t *tables) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     unsigned *err = P.ctrl + CW_ERR;
@@ -386,7 +387,8 @@ __global__ void plan_kernel(TrackParams P, const unsigned char *packed, int64_t 
         }
     }
     int64_t *unit_off = tables, *chunks = unit_off + P.n_designs + 1, *chunk_tiles = chunks + P.n_designs;
-    if (plan_units_hd(P.seg_off, P.n_designs, P.n_p, P.G, target_units, max_units, unit_off, chunks, chunk_tiles) < 0)
+    if (plan_units_hd(P.seg_off, P.n_designs, P.n_p, P.G, target_units, min_units, max_units, unit_off, chunks,
+                      chunk_tiles) < 0)
         atomicExch(err, (unsigned)CCT_ERR_ARG);
 }
 
@@ -451,7 +453,7 @@ int launch_track_async(const double *kls, const double *p0s, const int64_t *seg_
     P.record = nullptr;
     set_flow(P, sc + L.flow_off);
     CCT_TRY_CUDA(cudaMemsetAsync(sc, 0, 256, st));
-    plan_kernel<<<1, 32, 0, st>>>(P, static_cast<const unsigned char *>(packed), (int64_t)g_units_per_cta * grid,
+    plan_kernel<<<1, 32, 0, st>>>(P, static_cast<const unsigned char *>(packed), (int64_t)g_units_per_cta * grid, grid,
                                   max_units, reinterpret_cast<int64_t *>(sc + 256));
     CCT_TRY_CUDA(cudaGetLastError());
     cudaLaunchConfig_t cfg = {};

@@ -19,6 +19,7 @@ constexpr int kMaxGroup = 64 * kTrackWarps;   // particles per unit: 2 per lane 
 constexpr int kStateD = 24;          // doubles of RK4 state per particle
 constexpr int kMaxChunks = 4096;     // chunks per (design, block)
 constexpr int kUnitsPerCta = 8;      // default target units per CTA and stage (dynamic load balance)
+constexpr int kMinChunkTiles = 32;   // smallest chunk (tiles) a unit covers, given enough units for every CTA
 constexpr int kRing = 4;             // TMA ring depth (tiles)
 constexpr int kTrackUnroll = 8;      // unroll of the 4-segment loop of a sub-block (8: fully)
 constexpr int kGradUnroll = 4;       // the same in the adjoint's gradient sums
@@ -728,13 +729,14 @@ __host__ __device__ inline int64_t tiles_of(const int64_t *seg_off, int d) {
 
 // Units are (design, particle block of G, chunk of ct tiles).  Every chunk of every design
 // spans the same ct tiles (the last one of a design fewer), with ct chosen for about
-// target_units units and at most max_units.  Fills unit_off[n+1], chunks[n], chunk_tiles[n];
+// target_units units -- fewer if the chunks would then cover less than kMinChunkTiles tiles,
+// but not fewer than min_units (the CTAs) -- and at most max_units.  Fills unit_off[n+1], chunks[n], chunk_tiles[n];
 // returns the unit count, or -1 if one chunk per (design, block) is already more than
 // max_units.  The host plans cct_track's units with it, a one-thread kernel those of
 // cct_track_async.
 __host__ __device__ inline int64_t plan_units_hd(const int64_t *seg_off, int n_designs, int64_t n_p, int G,
-                                                 int64_t target_units, int64_t max_units, int64_t *unit_off,
-                                                 int64_t *chunks, int64_t *chunk_tiles) {
+                                                 int64_t target_units, int64_t min_units, int64_t max_units,
+                                                 int64_t *unit_off, int64_t *chunks, int64_t *chunk_tiles) {
     const int64_t blocks = (n_p + G - 1) / G;
     int64_t work = 0, max_nt = 1;
     for (int d = 0; d < n_designs; ++d) {
@@ -742,7 +744,9 @@ __host__ __device__ inline int64_t plan_units_hd(const int64_t *seg_off, int n_d
         work += blocks * nt;
         max_nt = hd_max(max_nt, nt);
     }
-    const int64_t target = hd_max(1, hd_min(target_units, max_units));
+    // no smaller chunks than kMinChunkTiles tiles, unless that leaves fewer units than min_units
+    const int64_t by_size = (work + kMinChunkTiles - 1) / kMinChunkTiles;
+    const int64_t target = hd_max(1, hd_min(hd_max(min_units, hd_min(target_units, by_size)), max_units));
     int64_t ct = hd_max(hd_max((work + target - 1) / target, (max_nt + kMaxChunks - 1) / kMaxChunks), 1);
     for (;;) {
         int64_t units = 0;
