@@ -232,7 +232,8 @@ def measure_tracking(args, dev, rank):
                     "gpairs_per_s": 512 * 4 * dsp.n_segments / tp64 / 1e9},
             "speedup_f32c_vs_f64": rp / rp64,
             "f32c_autotuned": tuned(dsp, pp, s32 // 2, 512)}
-    out["reference_speed_test"] = measure_speed_test(rank)
+    if not args.no_speed_test:
+        out["reference_speed_test"] = measure_speed_test(rank)
     if not args.no_adjoint:
         out["design_gradients"] = measure_design_grads(args, rank)
     if not args.no_generation:
@@ -591,6 +592,7 @@ def main():
     ap.add_argument("--track-steps", type=int, default=20, help="timed FP32c RK4 steps of the tracking slice")
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-generation", action="store_true")
+    ap.add_argument("--no-speed-test", action="store_true", help="skip the reference's own GPU speed-test slice")
     ap.add_argument("--adjoint-steps", type=int, default=32, help="RK4 steps of the design-gradient slice")
     ap.add_argument("--traffic", type=float, default=None,
                     help="DRAM bytes per launch of the timed kernel from an ncu capture (default: the committed "
