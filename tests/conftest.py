@@ -22,6 +22,15 @@ def golden():
 
 
 @pytest.fixture(scope="session")
+def golden_hust1():
+    """The gantry's first bending section from the reference (make_golden_hust1.py)."""
+    g = dict(np.load(os.path.join(GOLDEN, "golden_hust1.npz")))
+    with open(os.path.join(GOLDEN, "records_hust1.json")) as f:
+        g["records"] = json.load(f)["hust1_default"]
+    return g
+
+
+@pytest.fixture(scope="session")
 def records_json():
     with open(os.path.join(GOLDEN, "records.json")) as f:
         return json.load(f)

@@ -43,6 +43,14 @@ def test_hust2_section_with_qs(golden, prec, ptol, vtol):
 
 
 @pytest.mark.parametrize("prec,ptol,vtol", [("f64", POS_TOL_F64, VEL_RTOL_F64), ("f32c", POS_TOL_F32C, 1e-6)])
+def test_hust1_section_with_three_qs(golden_hust1, prec, ptol, vtol):
+    bl = HUST_SC_GANTRY().create_first_bending_part_beamline()
+    out = engine.track(engine.design_of(bl), golden_hust1["h1_particles_in"], float(golden_hust1["h1_length"][0]),
+                       0.1, prec)[0]
+    check(out, golden_hust1["h1_particles_out"], ptol, vtol)
+
+
+@pytest.mark.parametrize("prec,ptol,vtol", [("f64", POS_TOL_F64, VEL_RTOL_F64), ("f32c", POS_TOL_F32C, 1e-6)])
 def test_gantry_section(golden, prec, ptol, vtol):
     bl = W.build_gantry_section()
     out = engine.track(engine.design_of(bl), golden["gs_particles_in"], 3.5, 0.05, prec)[0]

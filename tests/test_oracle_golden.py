@@ -165,6 +165,19 @@ def test_track_hust2_ideal_matches_reference(golden, records_json):
     assert abs(out[2] - 5.0076184754665586e-05) < 1e-13
 
 
+def test_first_section_matches_reference(golden_hust1):
+    """The gantry's first bending section (12 CCT layers, 3 QS): fields and the RK4 track of
+    three protons at 100 mm steps over the whole section, bit for bit.  (The known answer printed
+    in gpu_accelerator.py:1535 was produced by an earlier revision of the section: its track is
+    4.15 m long, today's 4.82 m.)"""
+    bl = O.BeamlineOracle(oracle_records(golden_hust1["records"]))
+    B = np.array([bl.field_at(tuple(p)) for p in golden_hust1["h1_field_pts"]])
+    assert np.allclose(B, golden_hust1["h1_field_B"], rtol=1e-13, atol=1e-16)
+    L = float(golden_hust1["h1_length"][0])
+    for p_in, p_out in zip(golden_hust1["h1_particles_in"], golden_hust1["h1_particles_out"]):
+        assert np.array_equal(O.rk4_track(p_in, bl.field_at, L, 0.1), p_out)
+
+
 @pytest.mark.slow
 def test_track_single_dipole_two_protons_match_reference(golden):
     _, rec = single_dipole_record()
