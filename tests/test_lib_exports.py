@@ -70,3 +70,32 @@ def test_layer_records_checked_on_host(lib):
     bad = rec.copy()
     bad[0, 19] = 2.5                    # fractional winding number
     assert lib.cct_layer_segments(bad.ctypes.data_as(ctypes.c_void_p), 2) == -1
+
+
+def test_tracking_arguments_checked_on_host(lib):
+    """Argument errors of the tracking entry points are reported before any device work."""
+    dummy = ctypes.c_void_p(256)   # never dereferenced: every call below fails its checks first
+    args = dict(kls=None, p0s=None, seg_off=dummy, packed=None, qs=None, qs_off=dummy, n_designs=1,
+                particles=dummy, n=4, distance=1.0, footstep=0.01, precision=0, scratch=dummy, nbytes=1 << 20)
+
+    def track(**kw):
+        a = dict(args, **kw)
+        return lib.cct_track(a["kls"], a["p0s"], a["seg_off"], a["packed"], a["qs"], a["qs_off"], a["n_designs"],
+                             a["particles"], a["n"], a["distance"], a["footstep"], a["precision"], a["scratch"],
+                             a["nbytes"], None)
+
+    assert track(n_designs=0) == _lib.CCT_ERR_ARG
+    assert track(footstep=0.0) == _lib.CCT_ERR_ARG
+    assert track(distance=float("nan")) == _lib.CCT_ERR_ARG
+    assert track(precision=2) == _lib.CCT_ERR_ARG
+    assert track(particles=None) == _lib.CCT_ERR_ARG
+    assert track(precision=1, packed=None) == _lib.CCT_ERR_ARG
+    assert "packed" in _lib.last_error()
+    assert track(precision=1, packed=ctypes.c_void_p(300)) == _lib.CCT_ERR_ARG   # not 256-byte aligned
+    assert track(n=0) == _lib.CCT_OK                                              # nothing to track
+    assert lib.cct_track_async(None, None, dummy, None, None, dummy, 0, dummy, 4, 1.0, 0.01, 0, dummy,
+                               1 << 20, None) == _lib.CCT_ERR_ARG
+    assert lib.cct_track_async(None, None, dummy, None, None, dummy, 1, dummy, 4, 1.0, 0.01, 1, dummy,
+                               1 << 20, None) == _lib.CCT_ERR_ARG                 # FP32c without packed set
+    assert lib.cct_track_set_units_per_cta(65) == _lib.CCT_ERR_ARG
+    assert lib.cct_track_set_units_per_cta(-1) == _lib.CCT_ERR_ARG
