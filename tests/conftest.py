@@ -23,10 +23,13 @@ def golden():
 
 @pytest.fixture(scope="session")
 def golden_hust1():
-    """The gantry's first bending section from the reference (make_golden_hust1.py)."""
+    """The gantry's first bending section and the whole gantry from the reference
+    (make_golden_hust1.py)."""
     g = dict(np.load(os.path.join(GOLDEN, "golden_hust1.npz")))
     with open(os.path.join(GOLDEN, "records_hust1.json")) as f:
-        g["records"] = json.load(f)["hust1_default"]
+        recs = json.load(f)
+    g["records"] = recs["hust1_default"]
+    g["records_total"] = recs["total_default"]
     return g
 
 

@@ -5,8 +5,8 @@
 
 Outputs (small, committed): ``golden_hust1.npz`` (field points and fields, the ideal 215 MeV
 proton plus two beam protons before and after the reference's own RK4 track over the whole
-section at 100 mm steps) and ``records_hust1.json`` (the section's magnets as the reference
-built them).
+section at 100 mm steps; the same for the whole gantry with the ideal proton) and
+``records_hust1.json`` (the magnets as the reference built them).
 """
 from __future__ import annotations
 
@@ -49,6 +49,20 @@ def main():
     ParticleRunner.run_only(ps, bl, bl.get_length(), footstep=100 * MM, concurrency_level=3, report=False)
     print(f"hust1 default: tracked 3 protons in {time.time() - t0:.1f} s")
     arrays["h1_particles_out"] = particles_array(ps)
+    # the whole gantry (first section, the second section after it): placement, fields and
+    # the ideal proton tracked over the whole length at 100 mm
+    total = HUST_SC_GANTRY().create_total_beamline()
+    records["total_default"] = [record_of(m) for m in total.magnets]
+    arrays["tot_length"] = np.array([total.get_length()])
+    pts = np.array([[total.point_at(s).x, total.point_at(s).y, 0.004] for s in np.linspace(0.3, total.get_length() - 0.3, 8)])
+    arrays["tot_field_pts"] = pts
+    arrays["tot_field_B"] = field_points(total, pts)
+    tp = [ParticleFactory.create_proton_along(total, kinetic_MeV=215)]
+    arrays["tot_particles_in"] = particles_array(tp)
+    t0 = time.time()
+    ParticleRunner.run_only(tp, total, total.get_length(), footstep=100 * MM, concurrency_level=1, report=False)
+    print(f"total gantry: tracked the ideal proton in {time.time() - t0:.1f} s")
+    arrays["tot_particles_out"] = particles_array(tp)
     np.savez_compressed(os.path.join(HERE, "golden_hust1.npz"), **arrays)
     with open(os.path.join(HERE, "records_hust1.json"), "w") as f:
         json.dump(records, f, indent=1)

@@ -58,6 +58,16 @@ def test_first_section_placement(golden_hust1):
     assert abs(bl.get_length() - float(golden_hust1["h1_length"][0])) < 1e-12
 
 
+def test_total_gantry_placement(golden_hust1):
+    bl = HUST_SC_GANTRY().create_total_beamline()
+    recs = golden_hust1["records_total"]
+    assert len(bl.magnets) == len(recs) == 32
+    for m, r in zip(bl.magnets, recs):
+        params_match(m, r)
+        assert np.allclose(frame(m), np.array(r["frame"]), rtol=0, atol=1e-12)
+    assert abs(bl.get_length() - float(golden_hust1["tot_length"][0])) < 1e-12
+
+
 def test_design_population_placement(records_json):
     for d, kw in enumerate(W.design_population(2, seed=3)):
         bl = HUST_SC_GANTRY(**kw).create_second_bending_part_beamline()

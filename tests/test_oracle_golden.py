@@ -179,6 +179,17 @@ def test_first_section_matches_reference(golden_hust1):
 
 
 @pytest.mark.slow
+def test_total_gantry_matches_reference(golden_hust1):
+    """The whole gantry (32 magnets, 11.9 m): fields and the ideal proton's RK4 track at
+    100 mm steps, bit for bit."""
+    bl = O.BeamlineOracle(oracle_records(golden_hust1["records_total"]))
+    B = np.array([bl.field_at(tuple(p)) for p in golden_hust1["tot_field_pts"]])
+    assert np.allclose(B, golden_hust1["tot_field_B"], rtol=1e-13, atol=1e-16)
+    out = O.rk4_track(golden_hust1["tot_particles_in"][0], bl.field_at, float(golden_hust1["tot_length"][0]), 0.1)
+    assert np.array_equal(out, golden_hust1["tot_particles_out"][0])
+
+
+@pytest.mark.slow
 def test_track_single_dipole_two_protons_match_reference(golden):
     _, rec = single_dipole_record()
     m = O.CCTOracle(rec)
