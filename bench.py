@@ -34,9 +34,10 @@ if ROOT not in sys.path:
 N_POINTS = 1 << 20
 N_SEG = 46080
 FLOPS_PER_PAIR = 26
-# dram__bytes_read.sum + dram__bytes_write.sum of one field_f32c_kernel launch on the field map
-# (ncu --section MemoryWorkloadAnalysis ...; profiles/field_f32c_field_map.md): the 25 MB of
-# points and 1.7 MB of tiles read; the 25 MB of fields written are still in L2 at the end.
+# DRAM bytes (read + write) of one field_f32c_kernel launch on the field map, from an ncu
+# capture of this bench's field-map run (dram__bytes.sum.per_second x gpu__time_duration.sum):
+# the 25 MB of points and 1.7 MB of tiles read; the 25 MB of fields written are still in L2
+# when the kernel ends.
 FIELD_MAP_TRAFFIC_BYTES = 26.96e6
 METRIC = "Biot-Savart Gpairs/s & design-grads/s, 1 GB300: FP32+comp vs FP64 @1e-7 rel"
 WORKLOAD = "field_map: 2^20 points x 46080-segment single CCT dipole"
@@ -553,8 +554,8 @@ def run_ours(args):
                          "frac": achieved / peak32,
                          "traffic": args.traffic if args.traffic is not None else
                          (FIELD_MAP_TRAFFIC_BYTES if N_POINTS == 1 << 20 else None),
-                         "traffic_unit": "bytes per launch (dram read + write, ncu capture of this kernel on this "
-                                         "workload: profiles/field_f32c_field_map.md)",
+                         "traffic_unit": "bytes per launch (dram read + write, from an ncu capture of this kernel "
+                                         "on this workload)",
                          "peak_source": "measured in this run: best of scalar FFMA and packed FP32x2 FMA "
                                         "chains (cct_probe_fma_peak)",
                          "peak_scalar_ffma": peak32_scalar, "peak_packed_ffma2": peak32_packed,
