@@ -46,6 +46,7 @@ SIGNATURES = {
     "cct_probe_fma_peak": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_double)]),
     "cct_test_set_barrier_fault": (ctypes.c_int, [ctypes.c_int, ctypes.c_int]),
     "cct_test_set_flow_fault": (ctypes.c_int, [ctypes.c_int, ctypes.c_int]),
+    "cct_test_plan_units": (_i64, [_p, _i32, _i64, _i32, _i32, _i64, _p, _p, _p, ctypes.POINTER(ctypes.c_int32)]),
 }
 
 _lib = None

@@ -502,6 +502,31 @@ extern "C" int cct_test_set_barrier_fault(int phantom_blocks, int wait_ms) {
     return CCT_OK;
 }
 
+extern "C" int64_t cct_test_plan_units(const int64_t *seg_off, int32_t n_designs, int64_t n_particles,
+                                       int32_t precision, int32_t grid, int64_t max_units, int64_t *unit_off,
+                                       int64_t *chunks, int64_t *chunk_tiles, int32_t *group) {
+    // Test hook: the planner cct_track runs on the host, for a grid given by the caller.
+    using namespace cctgpu;
+    clear_error();
+    if (n_designs <= 0 || n_particles <= 0 || grid <= 0 || (precision != 0 && precision != 1)) {
+        set_error(CCT_ERR_ARG, "need designs, particles, a grid and precision 0 or 1");
+        return -2;
+    }
+    if (!seg_off || !unit_off || !chunks || !chunk_tiles || !group) {
+        set_error(CCT_ERR_ARG, "null offsets or tables");
+        return -2;
+    }
+    for (int d = 0; d < n_designs; ++d)
+        if (seg_off[d + 1] < seg_off[d]) {
+            set_error(CCT_ERR_ARG, "segment offsets decrease at design %d", d);
+            return -2;
+        }
+    const int G = group_size(precision, n_particles);
+    *group = G;
+    if (max_units <= 0) max_units = units_bound(n_designs, n_particles, G, grid);
+    return plan_units(seg_off, n_designs, n_particles, G, grid, max_units, unit_off, chunks, chunk_tiles);
+}
+
 // ---------------------------------------------------------------- asynchronous form, tuning
 extern "C" int cct_track_async(const double *d_kls, const double *d_p0s, const int64_t *d_seg_off,
                                const void *d_packed, const double *d_qs, const int64_t *d_qs_off, int32_t n_designs,

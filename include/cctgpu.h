@@ -314,6 +314,21 @@ int cct_test_set_barrier_fault(int phantom_blocks, int wait_ms);
  * Process-wide; not for production use. */
 int cct_test_set_flow_fault(int stages_ahead, int wait_ms);
 
+/* Test hook: the work split cct_track plans, computed on the host for a grid
+ * of `grid` CTAs (no device needed).  Writes the particle block size to
+ * *group and, per design d, unit_off[d] (first unit; unit_off[n_designs] =
+ * total), chunks[d] (segment chunks per particle block) and chunk_tiles[d]
+ * (tiles of 128 segments per chunk).  max_units <= 0 takes the bound that
+ * cct_track_scratch_bytes sizes for (units per CTA x grid, plus one chunk
+ * per design and particle block).  Returns the unit count, -1 if one chunk
+ * per (design, block) is more than max_units, -2 on bad arguments.  No
+ * counterpart in the reference. */
+int64_t cct_test_plan_units(const int64_t *seg_off, int32_t n_designs,
+                            int64_t n_particles, int32_t precision,
+                            int32_t grid, int64_t max_units,
+                            int64_t *unit_off, int64_t *chunks,
+                            int64_t *chunk_tiles, int32_t *group);
+
 #ifdef __cplusplus
 }
 #endif
