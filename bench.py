@@ -125,8 +125,8 @@ def run_reference(args):
         return
     cores = os.cpu_count() or 1
     n = args.ref_points
-    for _ in range(max(args.warmup, 0) and 1):
-        oracle_field_sample(max(cores * 4, 64), seed=100, processes=cores)
+    for k in range(max(args.warmup, 0)):   # untimed: a small sample each (pool start-up, page-in)
+        oracle_field_sample(max(cores * 4, 64), seed=100 + k, processes=cores)
     rates, times = [], []
     for k in range(args.steps):
         r, dt = oracle_field_sample(n, seed=200 + k, processes=cores)
