@@ -24,6 +24,7 @@ SIGNATURES = {
     "cct_f32c_packed_bytes": (_i64, [_p, _i32]),
     "cct_f32c_pack": (ctypes.c_int, [_p, _p, _p, _i32, _p, _i64, _p]),
     "cct_field_f32c": (ctypes.c_int, [_p, _i32, _p, _i32, _p, _i64, _p, _p]),
+    "cct_field_status": (ctypes.c_int, [_p]),
     "cct_field_host": (ctypes.c_int, [_p, _p, _i64, _p, _i32, _p, _i64, _p, _i32]),
     "cct_track_scratch_bytes": (_i64, [_i32, _i64]),
     "cct_track": (ctypes.c_int, [_p, _p, _p, _p, _p, _p, _i32, _p, _i64, _d, _d, _i32, _p, _i64, _p]),

@@ -101,6 +101,20 @@ int cct_field_f32c(const void *d_packed, int32_t design, const double *d_qs, int
     return launch_field_f32c(d_packed, design, d_qs, n_qs, d_points, n_points, d_B, static_cast<cudaStream_t>(stream));
 }
 
+int cct_field_status(void *stream) {
+    clear_error();
+    int s = CCT_OK;
+    const int rc = take_field_status(static_cast<cudaStream_t>(stream), &s);
+    if (rc != CCT_OK) return rc;
+    if (s == CCT_ERR_ARG)
+        return set_error(CCT_ERR_ARG, "an FP32c field call was given a buffer that is not a packed segment set, or a "
+                                      "design index the set does not hold (its fields are NaN)");
+    if (s == CCT_ERR_TIMEOUT)
+        return set_error(CCT_ERR_TIMEOUT, "an FP32c field call's tile copy did not land within the wait limit (its "
+                                          "fields are NaN)");
+    return s == CCT_OK ? CCT_OK : set_error(s, "field kernel status %d", s);
+}
+
 int cct_field_host(const double *h_kls, const double *h_p0s, int64_t n_seg, const double *h_qs, int32_t n_qs,
                    const double *h_points, int64_t n_points, double *h_B, int32_t precision) {
     clear_error();

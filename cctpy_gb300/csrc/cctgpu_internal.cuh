@@ -42,6 +42,8 @@ int launch_pack_f32c(const double *kls, const double *p0s, const int64_t *h_seg_
                      void *packed, int64_t packed_bytes, cudaStream_t st);
 int launch_field_f32c(const void *packed, int design, const double *qs, int n_qs, const double *pts,
                       int64_t n, double *B, cudaStream_t st);
+// Reads and clears the status the FP32c field kernels recorded on the current device; waits for st.
+int take_field_status(cudaStream_t st, int *status);
 
 struct TrackScratchLayout {
     int64_t state_off, partial_off, ctrl_off, flow_off, total;

@@ -388,6 +388,18 @@ __global__ void __launch_bounds__(kF32Block, kF32Blocks) field_f32c_kernel(const
     }
 }
 
+__device__ int g_field_status_taken;   // g_field_status as field_status_take_kernel last found it
+
+__global__ void field_status_take_kernel() { g_field_status_taken = atomicExch(&g_field_status, 0); }
+
+int take_field_status(cudaStream_t st, int *status) {
+    field_status_take_kernel<<<1, 1, 0, st>>>();
+    CCT_TRY_CUDA(cudaGetLastError());
+    CCT_TRY_CUDA(cudaMemcpyFromSymbolAsync(status, g_field_status_taken, sizeof(int), 0, cudaMemcpyDeviceToHost, st));
+    CCT_TRY_CUDA(cudaStreamSynchronize(st));
+    return CCT_OK;
+}
+
 int launch_field_f32c(const void *packed, int design, const double *qs, int n_qs, const double *pts, int64_t n,
                       double *B, cudaStream_t st) {
     if (n == 0) return CCT_OK;

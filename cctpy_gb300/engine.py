@@ -412,6 +412,15 @@ def field_at_points(ds: DesignSet, points, precision: str = "f64", design: int =
     return out
 
 
+def field_status() -> None:
+    """Raise if an FP32c field call on this device (any stream) since the last check was given
+    a buffer that is not a packed set or a design it does not hold (ValueError), or gave up
+    waiting for a tile copy (CctTimeoutError); the fields of such a call are NaN.  Clears the
+    status; waits for the current stream (cct_field_status)."""
+    _device()
+    _lib.check(_lib.load().cct_field_status(_stream()), "cct_field_status")
+
+
 _scratch_cache = {}
 
 

@@ -91,6 +91,14 @@ int cct_field_f32c(const void *d_packed, int32_t design,
                    const double *d_points, int64_t n_points, double *d_B,
                    void *stream);
 
+/* Status the cct_field_f32c kernels of the current device (every stream) have
+ * recorded since the last call, which clears it: CCT_OK; CCT_ERR_ARG if a
+ * call was given a buffer that is not a packed set, or a design index the set
+ * does not hold; CCT_ERR_TIMEOUT if a tile copy did not land within the wait
+ * limit.  The fields of such a call are NaN.  Waits for `stream`.  No
+ * counterpart in the reference (its kernels have no such failure). */
+int cct_field_status(void *stream);
+
 /* Host-buffer convenience form of cct_field_f64 / cct_field_f32c used as the
  * end-to-end call: copies h_kls/h_p0s/h_points to the device, evaluates, and
  * copies B back; synchronous.  precision: 0 = FP64, 1 = FP32-compensated.
