@@ -94,11 +94,12 @@ def segment_gradient(ds: engine.DesignSet, particles, distance: float, footstep:
     if prec is None:
         raise ValueError(f"precision must be 'f64' or 'f32c', not {precision!r}")
     packed = ds.packed().data_ptr() if prec == 1 else 0
-    sc = engine.scratch(nbytes, dev)
-    rc = lib.cct_track_adjoint(engine._ptr(ds.kls), engine._ptr(ds.p0s), engine._ptr(ds.seg_off), packed,
-                               engine._ptr(ds.qs), engine._ptr(ds.qs_off), ds.n_designs, p.data_ptr(), n_p,
-                               float(distance), float(footstep), prec, fr.data_ptr(), J.data_ptr(), grad.data_ptr(),
-                               int(checkpoint), sc.data_ptr(), int(nbytes), engine._stream())
+    with engine._scratch_lock:
+        sc = engine.scratch(nbytes, dev)
+        rc = lib.cct_track_adjoint(engine._ptr(ds.kls), engine._ptr(ds.p0s), engine._ptr(ds.seg_off), packed,
+                                   engine._ptr(ds.qs), engine._ptr(ds.qs_off), ds.n_designs, p.data_ptr(), n_p,
+                                   float(distance), float(footstep), prec, fr.data_ptr(), J.data_ptr(),
+                                   grad.data_ptr(), int(checkpoint), sc.data_ptr(), int(nbytes), engine._stream())
     _lib.check(rc, "cct_track_adjoint")
     g = grad[:ds.n_segments]
     return J.cpu().numpy(), (g if on_device else g.cpu().numpy()), p.cpu().numpy()

@@ -10,6 +10,7 @@ form is built on first use.  Torch provides device memory and the stream.
 from __future__ import annotations
 
 import ctypes
+import threading
 from typing import List, Optional, Sequence
 
 import numpy as np
@@ -422,9 +423,13 @@ def field_status() -> None:
 
 
 _scratch_cache = {}
+# One scratch buffer per device, shared by the synchronous calls below: ctypes releases the GIL
+# during a library call, so calls from several host threads take this lock around its use.
+_scratch_lock = threading.Lock()
 
 
 def scratch(nbytes: int, dev) -> torch.Tensor:
+    """The device's shared 256-byte-aligned scratch of at least nbytes (hold _scratch_lock)."""
     key = (dev.index,)
     buf = _scratch_cache.get(key)
     if buf is None or buf.numel() < nbytes + 256:
@@ -458,10 +463,11 @@ def track(ds: DesignSet, particles, distance: float, footstep: float, precision:
     packed = ds.packed() if prec == 1 else None
     nbytes = lib.cct_track_scratch_bytes(ds.n_designs, n_p)
     _lib.check(0 if nbytes >= 0 else _lib.CCT_ERR_ARG, "cct_track_scratch_bytes")
-    sc = scratch(nbytes, dev)
-    rc = lib.cct_track(_ptr(ds.kls), _ptr(ds.p0s), _ptr(ds.seg_off), 0 if packed is None else packed.data_ptr(),
-                       _ptr(ds.qs), _ptr(ds.qs_off), ds.n_designs, _ptr(p), n_p, float(distance), float(footstep),
-                       prec, sc.data_ptr(), int(nbytes), _stream())
+    with _scratch_lock:
+        sc = scratch(nbytes, dev)
+        rc = lib.cct_track(_ptr(ds.kls), _ptr(ds.p0s), _ptr(ds.seg_off), 0 if packed is None else packed.data_ptr(),
+                           _ptr(ds.qs), _ptr(ds.qs_off), ds.n_designs, _ptr(p), n_p, float(distance),
+                           float(footstep), prec, sc.data_ptr(), int(nbytes), _stream())
     _lib.check(rc, "cct_track")
     return p.cpu().numpy() if as_numpy else p
 
@@ -523,11 +529,12 @@ def autotune(ds: DesignSet, particles, footstep: float, precision: str = "f32c",
     prec, packed = _track_args(ds, precision)
     n = lib.cct_autotune_scratch_bytes(ds.n_designs, p.shape[1])
     _lib.check(0 if n >= 0 else _lib.CCT_ERR_ARG, "cct_autotune_scratch_bytes")
-    sc = scratch(int(n), dev)
     best = ctypes.c_int32(0)
-    rc = lib.cct_autotune(_ptr(ds.kls), _ptr(ds.p0s), _ptr(ds.seg_off), packed, _ptr(ds.qs), _ptr(ds.qs_off),
-                          ds.n_designs, p.data_ptr(), p.shape[1], float(footstep), prec, int(steps), sc.data_ptr(),
-                          int(n), ctypes.byref(best), _stream())
+    with _scratch_lock:
+        sc = scratch(int(n), dev)
+        rc = lib.cct_autotune(_ptr(ds.kls), _ptr(ds.p0s), _ptr(ds.seg_off), packed, _ptr(ds.qs), _ptr(ds.qs_off),
+                              ds.n_designs, p.data_ptr(), p.shape[1], float(footstep), prec, int(steps),
+                              sc.data_ptr(), int(n), ctypes.byref(best), _stream())
     _lib.check(rc, "cct_autotune")
     return int(best.value)
 
