@@ -86,3 +86,41 @@ def test_sharded_population_two_ranks():
         np.testing.assert_array_equal(res, want)
         assert empty.shape == (2, 3) and np.all(empty == 1)
         assert t == 1.5
+
+
+def _failing_eval(rows):
+    raise ValueError("design evaluation failed")
+
+
+def _worker_fail(rank, world, port, q):
+    import datetime
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    dist.init_process_group("gloo", rank=rank, world_size=world, timeout=datetime.timedelta(seconds=10))
+    try:
+        ev = ShardedEvaluator(_failing_eval if rank == 1 else _design_fields)
+        ev(np.array([[1000.0], [2000.0]]))
+        q.put((rank, "returned"))
+    except ValueError:          # the failing rank's own error
+        q.put((rank, "ValueError"))
+    except RuntimeError:        # the survivor's failed gather (torch's distributed errors derive from it)
+        q.put((rank, "RuntimeError"))
+    finally:
+        dist.destroy_process_group()
+
+
+def test_a_failing_rank_ends_the_gather_with_an_error():
+    """A rank whose evaluation raises leaves the gather; the other rank's gather then fails
+    (gloo: the peer closed its connection; otherwise the process group's 10 s timeout) instead
+    of waiting for ever."""
+    world = 2
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_worker_fail, args=(r, world, port, q)) for r in range(world)]
+    for p in procs:
+        p.start()
+    got = dict(q.get(timeout=120) for _ in range(world))
+    for p in procs:
+        p.join(timeout=60)
+    assert got[1] == "ValueError"
+    assert got[0] == "RuntimeError"
