@@ -15,7 +15,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 def declared_functions():
     text = open(os.path.join(ROOT, "include", "cctgpu.h")).read()
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
-    return sorted(set(re.findall(r"^\s*(?:int|int64_t|void)\s+\**(cct_\w+)\s*\(", text, flags=re.M)))
+    return sorted(set(re.findall(r"^\s*(?:int|int32_t|int64_t|void|double)\s+\**(cct_\w+)\s*\(", text, flags=re.M)))
 
 
 @pytest.fixture(scope="module")
@@ -99,3 +99,20 @@ def test_tracking_arguments_checked_on_host(lib):
                                1 << 20, None) == _lib.CCT_ERR_ARG                 # FP32c without packed set
     assert lib.cct_track_set_units_per_cta(65) == _lib.CCT_ERR_ARG
     assert lib.cct_track_set_units_per_cta(-1) == _lib.CCT_ERR_ARG
+
+
+def test_every_exported_entry_point_is_declared(lib):
+    """The reverse direction: no cct_* symbol leaves the library without a declaration in the
+    header and a ctypes signature (dynamic symbol table, read with nm)."""
+    import shutil
+    import subprocess
+    nm = shutil.which("nm")
+    if nm is None:
+        pytest.skip("nm not available")
+    out = subprocess.run([nm, "-D", "--defined-only", _lib.LIB_PATH], capture_output=True, text=True,
+                         check=True).stdout
+    exported = sorted({line.split()[-1] for line in out.splitlines()
+                       if line.split() and line.split()[-1].startswith("cct_")})
+    assert exported, "no cct_ symbols exported"
+    assert set(exported) == set(declared_functions())
+    assert set(exported) == set(_lib.SIGNATURES)
