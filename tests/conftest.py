@@ -52,3 +52,23 @@ def oracle_records(recs):
         else:
             out.append(O.qs_record(fr, r["length"], r["gradient"], r["second_gradient"], r["aperture_radius"]))
     return out
+
+
+def reference_design(recs):
+    """(kls (N, 3), p0s (N, 3), analytic records (M, 16)) of a magnet list as cctpy itself
+    places it: the oracle's segment generation (a plain-float restatement of cct.py:87-164,
+    :423-457, bitwise equal to the reference) from the frames cctpy recorded.  These arrays do
+    not depend on the host's BLAS, unlike the package's own placement, whose least-squares
+    circle fit (numpy, as cctpy's base_utils.py:124-151) lands frames a few 1e-13 m apart on
+    different CPUs."""
+    from oracle import cct_oracle as O
+    kls, p0s, qs = [], [], []
+    for r in oracle_records(recs):
+        if r["kind"] == "cct":
+            k, p = O.cct_segments_global(r)
+            kls.append(k)
+            p0s.append(p)
+        else:
+            qs.append(O.QSOracle(r).to_array())
+    return (np.ascontiguousarray(np.concatenate(kls)), np.ascontiguousarray(np.concatenate(p0s)),
+            np.ascontiguousarray(np.array(qs).reshape(-1, 16)))

@@ -1,9 +1,9 @@
 """Generate the golden fixtures of the parity tests from the cctpy reference itself.
 
-Run in a container where the cctpy sources are mounted (default
-``/root/reference``; override with ``CCTPY_REFERENCE``):
+Run where the cctpy sources are available, with ``CCTPY_REFERENCE`` set to the
+directory that holds cctpy's ``final_code/``:
 
-    python tests/golden/make_golden.py
+    CCTPY_REFERENCE=<cctpy checkout> python tests/golden/make_golden.py
 
 The reference is imported unmodified with two harness-side shims:
 matplotlib is stubbed (every package module imports pyplot at top level but
@@ -29,10 +29,13 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
 from cctpy_gb300 import workloads  # noqa: E402
 
-REF = os.environ.get("CCTPY_REFERENCE", "/root/reference")
+REF = os.environ.get("CCTPY_REFERENCE", "")
 
 
 def load_reference():
+    if not REF or not os.path.isdir(os.path.join(REF, "final_code")):
+        raise SystemExit("set CCTPY_REFERENCE to the directory holding cctpy's final_code/ "
+                         f"(got {REF!r})")
     for name in ["matplotlib", "matplotlib.pyplot", "mpl_toolkits", "mpl_toolkits.mplot3d"]:
         sys.modules[name] = types.ModuleType(name)
     sys.modules["matplotlib"].pyplot = sys.modules["matplotlib.pyplot"]

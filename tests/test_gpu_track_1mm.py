@@ -1,0 +1,65 @@
+"""Tracking parity at the workloads' own 1 mm RK4 step against tracks cctpy computed itself
+(tests/golden/make_golden_1mm.py): the 597 600-segment gantry section with 8 protons and two
+designs of the seeded population with 4 protons each, over a 1.0 m window from s = 1.9 m on
+the design orbit (the end of the entrance drift and the first dipole's entrance), 1000 RK4
+steps.  The package builds the beamlines as a user would; both precisions are held to the
+tolerances of the other tracking tests, and the FP64 tracks on cctpy's own segment placement
+(`reference_design`) to the drop-in's 1e-12 m."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+from cctpy_gb300 import HUST_SC_GANTRY, engine, workloads as W
+from tests.conftest import GOLDEN, reference_design
+
+TOL = {"f64": (1e-9, 1e-9), "f32c": (1e-6, 1e-6)}   # position (m), velocity (relative to |v|)
+REF_POS_TOL = 1e-12
+
+
+@pytest.fixture(scope="module")
+def g1mm():
+    g = dict(np.load(os.path.join(GOLDEN, "golden_1mm.npz")))
+    with open(os.path.join(GOLDEN, "records_1mm.json")) as f:
+        g["records"] = json.load(f)
+    return g
+
+
+def _check(out, want, pos_tol, vel_rtol):
+    assert np.abs(out[:, 0:3] - want[:, 0:3]).max() <= pos_tol
+    assert np.abs(out[:, 3:6] - want[:, 3:6]).max() <= vel_rtol * np.abs(want[:, 3:6]).max()
+    assert np.array_equal(out[:, 6:9], want[:, 6:9])
+    np.testing.assert_allclose(out[:, 9], want[:, 9], rtol=1e-15)
+
+
+@pytest.mark.parametrize("prec", ["f64", "f32c"])
+def test_gantry_section_1mm(g1mm, prec):
+    _, window, step = g1mm["window"]
+    out = engine.track(engine.design_of(W.build_gantry_section()), g1mm["gs1_particles_in"], window, step, prec)[0]
+    _check(out, g1mm["gs1_particles_out"], *TOL[prec])
+
+
+@pytest.mark.parametrize("prec", ["f64", "f32c"])
+def test_design_population_1mm_one_launch(g1mm, prec):
+    _, window, step = g1mm["window"]
+    bls = [HUST_SC_GANTRY(**kw).create_second_bending_part_beamline() for kw in W.design_population(2, seed=3)]
+    parts = np.stack([g1mm["dp1mm0_particles_in"], g1mm["dp1mm1_particles_in"]])
+    out = engine.track(engine.design_set_of(bls), parts, window, step, prec)
+    for d in range(2):
+        _check(out[d], g1mm[f"dp1mm{d}_particles_out"], *TOL[prec])
+
+
+def test_f64_on_reference_segments_1mm(g1mm):
+    _, window, step = g1mm["window"]
+    recs = g1mm["records"]
+    sets = [reference_design(recs["gantry_section"])] + [reference_design(r) for r in recs["design_population"]]
+    for k, (pin, pout) in enumerate([("gs1_particles_in", "gs1_particles_out"),
+                                     ("dp1mm0_particles_in", "dp1mm0_particles_out"),
+                                     ("dp1mm1_particles_in", "dp1mm1_particles_out")]):
+        out = engine.track(engine.DesignSet([sets[k]]), g1mm[pin], window, step, "f64")[0]
+        _check(out, g1mm[pout], REF_POS_TOL, 1e-12)
