@@ -34,6 +34,8 @@ SIGNATURES = {
     "cct_track_status": (ctypes.c_int, [_p, _p]),
     "cct_track_set_units_per_cta": (ctypes.c_int, [_i32]),
     "cct_track_units_per_cta": (_i32, []),
+    "cct_track_set_particle_block": (ctypes.c_int, [_i32]),
+    "cct_track_particle_block": (_i32, []),
     "cct_autotune_scratch_bytes": (_i64, [_i32, _i64]),
     "cct_autotune": (ctypes.c_int, [_p, _p, _p, _p, _p, _p, _i32, _p, _i64, _d, _i32, _i32, _p, _i64,
                                     ctypes.POINTER(ctypes.c_int32), _p]),

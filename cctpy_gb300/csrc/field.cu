@@ -282,6 +282,7 @@ constexpr int kF32Ppt = 3;
 constexpr int kF32Blocks = 3;
 constexpr int kF32Unroll = 8;
 constexpr int kStages = 3;
+constexpr bool kF32Rcp = false;   // |r|^-3 as rsqrt x rcp (tile.cuh inv_r3)
 constexpr uint32_t kWaitPolls = 1u << 22;
 
 __device__ int g_field_status;   // last non-OK status seen by a field kernel (sticky)
@@ -352,7 +353,7 @@ __global__ void __launch_bounds__(kF32Block, kF32Blocks) field_f32c_kernel(const
             failed = true;
             break;
         }
-        tile_f32c_smem<kF32Ppt, kF32Unroll>(buf[s], &spt[0][0][tid], kF32Ppt * kF32Block, kF32Block, acc);
+        tile_f32c_smem<kF32Ppt, kF32Unroll, kF32Rcp>(buf[s], &spt[0][0][tid], kF32Ppt * kF32Block, kF32Block, acc);
         if (cctdev::ring_release_last(&released[s], kWarps) && t + kStages < nt) {
             last_issued[s] = t + kStages;
             cctdev::fence_proxy_async();

@@ -66,6 +66,23 @@ __device__ __forceinline__ float rsqrt_mufu(float x) {
     asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
     return y;
 }
+__device__ __forceinline__ float rcp_mufu(float x) {
+    float y;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+// |r|^-3 of two packed squared distances.  RCP = false: rsqrt cubed (MUFU rsqrt, two FMA-pipe
+// multiplies); RCP = true: rsqrt(r^2) x rcp(r^2) (two MUFU operations, one multiply), which
+// moves one of the pair's FMA-pipe operations to the MUFU pipe.
+template <bool RCP>
+__device__ __forceinline__ f2 inv_r3(f2 r2) {
+    float a, b;
+    f2_unpack(r2, a, b);
+    const f2 inv = f2_pack(rsqrt_mufu(a), rsqrt_mufu(b));
+    if (RCP) return f2_mul(inv, f2_pack(rcp_mufu(a), rcp_mufu(b)));
+    return f2_mul(f2_mul(inv, inv), inv);
+}
 
 // Kahan step: (S, C) += s
 __device__ __forceinline__ void kahan_add(float &S, float &C, float s) {
@@ -113,23 +130,23 @@ __device__ __forceinline__ void tile_offsets(const TileHeader *h, const float (&
         }
 }
 
-template <int PPT, int JU>
+template <int PPT, int JU, bool RCP>
 __device__ __forceinline__ void tile_pairs(const unsigned char *tile, const f2 (&q)[PPT][3], F32cAcc<PPT> &acc,
                                            int g0, int g1);
 
-template <int PPT, int JU = 1>
+template <int PPT, int JU = 1, bool RCP = false>
 __device__ __forceinline__ void tile_f32c(const unsigned char *tile, const float (&ph)[PPT][3],
                                           const float (&pl)[PPT][3], F32cAcc<PPT> &acc, int g0 = 0,
                                           int g1 = kTile / 4) {
     f2 q[PPT][3];
     tile_offsets<PPT>(reinterpret_cast<const TileHeader *>(tile), ph, pl, q);
-    tile_pairs<PPT, JU>(tile, q, acc, g0, g1);
+    tile_pairs<PPT, JU, RCP>(tile, q, acc, g0, g1);
 }
 
 // The same with the point's double-float coordinates kept in shared memory: component c
 // (hi x, y, z, lo x, y, z) of point i at sp[c * c_stride + i * i_stride], so that they hold
 // no registers during the segment loop.
-template <int PPT, int JU = 1>
+template <int PPT, int JU = 1, bool RCP = false>
 __device__ __forceinline__ void tile_f32c_smem(const unsigned char *tile, const float *sp, int c_stride, int i_stride,
                                                F32cAcc<PPT> &acc, int g0 = 0, int g1 = kTile / 4) {
     float ph[PPT][3], pl[PPT][3];
@@ -142,10 +159,10 @@ __device__ __forceinline__ void tile_f32c_smem(const unsigned char *tile, const 
         }
     f2 q[PPT][3];
     tile_offsets<PPT>(reinterpret_cast<const TileHeader *>(tile), ph, pl, q);
-    tile_pairs<PPT, JU>(tile, q, acc, g0, g1);
+    tile_pairs<PPT, JU, RCP>(tile, q, acc, g0, g1);
 }
 
-template <int PPT, int JU>
+template <int PPT, int JU, bool RCP>
 __device__ __forceinline__ void tile_pairs(const unsigned char *tile, const f2 (&q)[PPT][3], F32cAcc<PPT> &acc,
                                            int g0, int g1) {
     const TileHeader *h = reinterpret_cast<const TileHeader *>(tile);
@@ -182,10 +199,7 @@ __device__ __forceinline__ void tile_pairs(const unsigned char *tile, const f2 (
                 for (int i = 0; i < PPT; ++i) {
                     const f2 rx = f2_sub(q[i][0], px), ry = f2_sub(q[i][1], py), rz = f2_sub(q[i][2], pz);
                     const f2 r2 = f2_fma(rx, rx, f2_fma(ry, ry, f2_mul(rz, rz)));
-                    float a, b;
-                    f2_unpack(r2, a, b);
-                    const f2 inv = f2_pack(rsqrt_mufu(a), rsqrt_mufu(b));
-                    const f2 inv3 = f2_mul(f2_mul(inv, inv), inv);
+                    const f2 inv3 = inv_r3<RCP>(r2);
                     A[i][0] = f2_fma(kx, inv3, A[i][0]);
                     A[i][1] = f2_fma(ky, inv3, A[i][1]);
                     A[i][2] = f2_fma(kz, inv3, A[i][2]);

@@ -182,8 +182,8 @@ TrackScratchLayout track_scratch_layout(int n_designs, int64_t n_particles, int6
 }
 
 // Particles per unit: FP64 keeps 32 (warps split the tiles); FP32c takes the block size that
-// needs the fewest particle slots (blocks x G), the largest of those: e.g. 96 particles run as
-// one block of 128 (warps take half tiles) rather than 64 + 32 (quarter tiles), 9 % faster.
+// needs the fewest particle slots (blocks x G), the largest of those: e.g. 100 particles run as
+// one block of 128 rather than two of 64 (the same slots), 96 as three blocks of 32.
 int group_size(int precision, int64_t n_p) {
     if (precision == 0) return 32;
     int best = kMaxGroup;
@@ -196,6 +196,16 @@ int group_size(int precision, int64_t n_p) {
         }
     }
     return best;
+}
+
+int g_particle_block = 0;   // FP32c particle block set by hand or by cct_autotune (0: group_size's choice)
+
+// Particle block of the forward tracking entry points: the process-wide setting for FP32c if
+// one is made, else group_size's.  (The adjoint keeps group_size's, which its scratch query
+// assumes.)
+int track_group(int precision, int64_t n_p) {
+    if (precision == 1 && g_particle_block != 0) return g_particle_block;
+    return group_size(precision, n_p);
 }
 
 int track_grid(int *grid_out) {
@@ -242,7 +252,7 @@ int64_t track_scratch_bound(int n_designs, int64_t n_particles) {
     }
     int64_t best = 0;
     for (int prec = 0; prec < 2; ++prec) {
-        const int G = group_size(prec, n_particles);
+        const int G = track_group(prec, n_particles);
         const int64_t t = track_scratch_layout(n_designs, n_particles, units_bound(n_designs, n_particles, G, grid), G).total;
         if (t > best) best = t;
     }
@@ -287,7 +297,7 @@ static int run_track(const double *kls, const double *p0s, const int64_t *seg_of
     int grid = 0;
     const int rc = track_grid(&grid);
     if (rc != CCT_OK) return rc;
-    const int G = group_size(precision, n_particles);
+    const int G = track_group(precision, n_particles);
     int64_t *unit_off = tables, *chunks = unit_off + n_designs + 1, *chunk_tiles = chunks + n_designs;
     const int64_t n_units = plan_units(hoff, n_designs, n_particles, G, grid,
                                        units_fitting(n_designs, n_particles, G, scratch_bytes), unit_off, chunks,
@@ -410,7 +420,7 @@ int launch_track_async(const double *kls, const double *p0s, const int64_t *seg_
     const int grid = g_async_grid[dev];
     unsigned char *sc = static_cast<unsigned char *>(scratch);
     if (reinterpret_cast<uintptr_t>(sc) % 256) return set_error(CCT_ERR_ARG, "tracking scratch must be 256-byte aligned");
-    const int G = group_size(precision, n_p);
+    const int G = track_group(precision, n_p);
     const int64_t max_units = units_fitting(n_designs, n_p, G, scratch_bytes);
     if (max_units < (int64_t)n_designs * ((n_p + G - 1) / G))
         return set_error(CCT_ERR_ARG, "%d designs x %lld particles need at least %lld bytes of tracking scratch, %lld given",
@@ -521,7 +531,7 @@ extern "C" int64_t cct_test_plan_units(const int64_t *seg_off, int32_t n_designs
             set_error(CCT_ERR_ARG, "segment offsets decrease at design %d", d);
             return -2;
         }
-    const int G = group_size(precision, n_particles);
+    const int G = track_group(precision, n_particles);
     *group = G;
     if (max_units <= 0) max_units = units_bound(n_designs, n_particles, G, grid);
     return plan_units(seg_off, n_designs, n_particles, G, grid, max_units, unit_off, chunks, chunk_tiles);
@@ -560,10 +570,58 @@ extern "C" int cct_track_set_units_per_cta(int32_t units_per_cta) {
 
 extern "C" int32_t cct_track_units_per_cta(void) { return cctgpu::g_units_per_cta; }
 
-namespace cctgpu {
-static const int kTuneCandidates[] = {2, 4, 8, 16, 32};
-static int64_t up256(int64_t b) { return (b + 255) / 256 * 256; }
+extern "C" int cct_track_set_particle_block(int32_t particles) {
+    cctgpu::clear_error();
+    if (particles != 0 && particles != 32 && particles != 64 && particles != 128 && particles != 256)
+        return cctgpu::set_error(CCT_ERR_ARG, "particle block %d (32, 64, 128 or 256; 0 = automatic)", particles);
+    cctgpu::g_particle_block = particles;
+    return CCT_OK;
 }
+
+extern "C" int32_t cct_track_particle_block(void) { return cctgpu::g_particle_block; }
+
+namespace cctgpu {
+static const int kTuneUnits[] = {2, 4, 8, 16, 32};
+static const int kTuneBlocks[] = {32, 64, 128, 256};
+constexpr int kNumTuneUnits = (int)(sizeof kTuneUnits / sizeof kTuneUnits[0]);
+constexpr int kNumTuneBlocks = (int)(sizeof kTuneBlocks / sizeof kTuneBlocks[0]);
+static int64_t up256(int64_t b) { return (b + 255) / 256 * 256; }
+
+// Particle blocks worth timing for n_p particles of one design: the automatic choice, and every
+// block size up to the smallest that holds all n_p (a larger one only adds idle lanes).
+static int tune_blocks(int precision, int64_t n_p, int *out) {
+    if (precision == 0) {
+        out[0] = 0;
+        return 1;
+    }
+    int n = 0;
+    out[n++] = 0;
+    for (int i = 0; i < kNumTuneBlocks; ++i) {
+        out[n++] = kTuneBlocks[i];
+        if (kTuneBlocks[i] >= n_p) break;
+    }
+    return n;
+}
+
+// Scratch of the largest candidate split (tracking scratch of every candidate, plus a copy of
+// the particle records).
+static int64_t autotune_bytes(int n_designs, int64_t n_p) {
+    const int saved_u = g_units_per_cta, saved_g = g_particle_block;
+    int blocks[kNumTuneBlocks + 1];
+    int64_t best = 0;
+    for (int prec = 0; prec < 2; ++prec) {
+        const int nb = tune_blocks(prec, n_p, blocks);
+        for (int i = 0; i < nb; ++i) {
+            g_particle_block = blocks[i];
+            g_units_per_cta = kTuneUnits[kNumTuneUnits - 1];
+            best = std::max(best, track_scratch_bound(n_designs, n_p));
+        }
+    }
+    g_units_per_cta = saved_u;
+    g_particle_block = saved_g;
+    return up256(80 * (int64_t)n_designs * n_p) + best;
+}
+}  // namespace cctgpu
 
 extern "C" int64_t cct_autotune_scratch_bytes(int32_t n_designs, int64_t n_particles) {
     using namespace cctgpu;
@@ -572,11 +630,7 @@ extern "C" int64_t cct_autotune_scratch_bytes(int32_t n_designs, int64_t n_parti
         set_error(CCT_ERR_ARG, "need at least one design and particle");
         return -1;
     }
-    const int saved = g_units_per_cta;
-    g_units_per_cta = kTuneCandidates[sizeof kTuneCandidates / sizeof kTuneCandidates[0] - 1];
-    const int64_t t = track_scratch_bound(n_designs, n_particles);
-    g_units_per_cta = saved;
-    return up256(80 * (int64_t)n_designs * n_particles) + t;
+    return autotune_bytes(n_designs, n_particles);
 }
 
 extern "C" int cct_autotune(const double *d_kls, const double *d_p0s, const int64_t *d_seg_off, const void *d_packed,
@@ -588,23 +642,28 @@ extern "C" int cct_autotune(const double *d_kls, const double *d_p0s, const int6
     clear_error();
     if (n_designs <= 0 || n_particles <= 0 || steps < 1 || !(footstep > 0.0))
         return set_error(CCT_ERR_ARG, "need designs, particles, steps >= 1 and footstep > 0");
+    if (precision != 0 && precision != 1) return set_error(CCT_ERR_ARG, "precision must be 0 (FP64) or 1 (FP32c)");
     if (!d_particles || !d_scratch || !units_per_cta_out) return set_error(CCT_ERR_ARG, "null particles, scratch or output");
+    const int64_t need = autotune_bytes(n_designs, n_particles);
+    if (scratch_bytes < need)
+        return set_error(CCT_ERR_ARG, "autotune needs %lld bytes of scratch, %lld given", (long long)need,
+                         (long long)scratch_bytes);
     const int64_t copy = up256(80 * (int64_t)n_designs * n_particles);
-    if (scratch_bytes < cct_autotune_scratch_bytes(n_designs, n_particles))
-        return set_error(CCT_ERR_ARG, "autotune needs %lld bytes of scratch, %lld given",
-                         (long long)cct_autotune_scratch_bytes(n_designs, n_particles), (long long)scratch_bytes);
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     unsigned char *sc = static_cast<unsigned char *>(d_scratch);
     double *work = reinterpret_cast<double *>(sc);
-    const int saved = g_units_per_cta;
+    const int saved_u = g_units_per_cta, saved_g = g_particle_block;
+    int blocks[kNumTuneBlocks + 1];
+    const int nb = tune_blocks(precision, n_particles, blocks);
     cudaEvent_t a = nullptr, b = nullptr;
     CCT_TRY_CUDA(cudaEventCreate(&a));
     CCT_TRY_CUDA(cudaEventCreate(&b));
     float best_ms = 3.4e38f;
-    int best = saved, rc = CCT_OK;
-    const int n_cand = (int)(sizeof kTuneCandidates / sizeof kTuneCandidates[0]);
-    for (int i = -1; i < n_cand && rc == CCT_OK; ++i) {        // i = -1: warm-up with the current setting
-        g_units_per_cta = i < 0 ? saved : kTuneCandidates[i];
+    int best_u = saved_u, best_g = saved_g, rc = CCT_OK;
+    // candidate -1: warm-up with the current setting; then every (particle block, units per CTA)
+    for (int c = -1; c < nb * kNumTuneUnits && rc == CCT_OK; ++c) {
+        g_units_per_cta = c < 0 ? saved_u : kTuneUnits[c % kNumTuneUnits];
+        g_particle_block = c < 0 ? saved_g : blocks[c / kNumTuneUnits];
         cudaError_t e = cudaMemcpyAsync(work, d_particles, 80 * (size_t)n_designs * n_particles,
                                         cudaMemcpyDeviceToDevice, st);
         if (e == cudaSuccess) e = cudaEventRecord(a, st);
@@ -623,15 +682,17 @@ extern "C" int cct_autotune(const double *d_kls, const double *d_p0s, const int6
             rc = check_cuda(e, "autotune timing");
             break;
         }
-        if (i >= 0 && ms < best_ms) {
+        if (c >= 0 && ms < best_ms) {
             best_ms = ms;
-            best = kTuneCandidates[i];
+            best_u = g_units_per_cta;
+            best_g = g_particle_block;
         }
     }
     cudaEventDestroy(a);
     cudaEventDestroy(b);
-    g_units_per_cta = rc == CCT_OK ? best : saved;
-    if (rc == CCT_OK) *units_per_cta_out = best;
+    g_units_per_cta = rc == CCT_OK ? best_u : saved_u;
+    g_particle_block = rc == CCT_OK ? best_g : saved_g;
+    if (rc == CCT_OK) *units_per_cta_out = best_u;
     return rc;
 }
 
@@ -643,10 +704,12 @@ extern "C" int cct_autotune(const double *d_kls, const double *d_p0s, const int6
 // its hot path (an allocation there can fail mid-run or stall the device), or a plain C
 // caller that owns only the buffers it was handed.  cct_track_static_scratch gives them
 // the tracking kernel with its scratch in a fixed, file-scope device array instead of a
-// caller-provided buffer.  The array is created when the library is loaded, on every GPU
-// the process uses, and stays allocated until the process exits; its size bounds the
-// problem (see cctgpu.h).  All calls share it, so calls whose kernels overlap on the GPU
-// race on it; each call rewrites every word it reads before the kernel starts.
+// caller-provided buffer.  The array takes its device memory when this file's CUDA module is
+// loaded on a device -- under lazy module loading, its first use there -- and keeps it until
+// the process exits; cct_track_static_scratch_bytes() looks the array up on the current
+// device so that a start-up call places it before the caller reserves its memory.  Its size
+// bounds the problem (see cctgpu.h).  All calls share it, so calls whose kernels overlap on
+// the GPU race on it; each call rewrites every word it reads before the kernel starts.
 // ============================================================================
 namespace cctgpu {
 
@@ -659,7 +722,8 @@ static void *g_static_scratch_addr[kStaticMaxDevices];
 static std::mutex g_static_scratch_mutex;
 
 // Device address of the static scratch on the current device.  The first call on a
-// device looks the symbol up (cudaGetSymbolAddress) with that device current.
+// device looks the symbol up (cudaGetSymbolAddress) with that device current and keeps the
+// address for the life of the process (a cudaDeviceReset of that device would make it stale).
 static int static_scratch_address(void **out) {
     int dev = 0;
     CCT_TRY_CUDA(cudaGetDevice(&dev));
@@ -695,7 +759,19 @@ static int launch_track_static(const double *kls, const double *p0s, const int64
 
 }  // namespace cctgpu
 
-extern "C" int64_t cct_track_static_scratch_bytes(void) { return cctgpu::kStaticScratchBytes; }
+extern "C" int64_t cct_track_static_scratch_bytes(void) {
+    // With a device visible, also look the array up on the current device: that loads this
+    // file's module there and so commits the array, letting a start-up call place it before
+    // the application reserves its memory.  Without a device only the size is returned.
+    int n = 0;
+    if (cudaGetDeviceCount(&n) == cudaSuccess && n > 0) {
+        void *p = nullptr;
+        if (cctgpu::static_scratch_address(&p) != CCT_OK) cctgpu::clear_error();
+    } else {
+        (void)cudaGetLastError();
+    }
+    return cctgpu::kStaticScratchBytes;
+}
 
 extern "C" int cct_track_static_scratch(const double *d_kls, const double *d_p0s, const int64_t *d_seg_off,
                                         const void *d_packed, const double *d_qs, const int64_t *d_qs_off,

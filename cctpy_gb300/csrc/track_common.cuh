@@ -23,6 +23,7 @@ constexpr int kMinChunkTiles = 32;   // smallest chunk (tiles) a unit covers, gi
 constexpr int kRing = 4;             // TMA ring depth (tiles)
 constexpr int kTrackUnroll = 8;      // unroll of the 4-segment loop of a sub-block (8: fully)
 constexpr int kGradUnroll = 4;       // the same in the adjoint's gradient sums
+constexpr bool kTrackRcp = false;     // |r|^-3 as rsqrt x rcp in the tracking field sums (tile.cuh inv_r3)
 constexpr int kRedDoubles = kMaxGroup * 3;   // per-CTA reduction buffer: S slices x G particles x 3
 constexpr uint32_t kTmaPolls = 1u << 22;
 
@@ -424,7 +425,7 @@ static __device__ int64_t unit_sum_f32c(const TrackParams &P, const PointSrc &sr
             break;
         }
         if (GRAD) tile_grad_f32c<PPT, kGradUnroll>(sm.ring[s], ph, pl, a, acc, g0, g1);
-        else tile_f32c<PPT, kTrackUnroll>(sm.ring[s], ph, pl, acc, g0, g1);
+        else tile_f32c<PPT, kTrackUnroll, kTrackRcp>(sm.ring[s], ph, pl, acc, g0, g1);
         if (cctdev::ring_release_last(&sm.released[s], kTrackWarps) && t + kRing < nt) {
             sm.last_issued[s] = k + kRing;
             cctdev::fence_proxy_async();
@@ -774,7 +775,9 @@ extern int g_units_per_cta;
 extern int g_test_phantom_blocks;
 extern int g_test_flow_skew;
 extern long long g_wait_ms;
+extern int g_particle_block;
 int group_size(int precision, int64_t n_p);
+int track_group(int precision, int64_t n_p);
 int track_grid(int *grid_out);
 int64_t plan_units(const int64_t *hoff, int n_designs, int64_t n_p, int G, int grid, int64_t max_units, int64_t *unit_off,
                    int64_t *chunks, int64_t *chunk_tiles);

@@ -516,9 +516,10 @@ class TrackLaunch:
 
 
 def autotune(ds: DesignSet, particles, footstep: float, precision: str = "f32c", steps: int = 4) -> int:
-    """Time `steps` RK4 steps of this problem for several work splits (units of design x
-    particle block x segment chunk per CTA), keep the fastest for later tracking calls of the
-    process and return it (cct_autotune)."""
+    """Time `steps` RK4 steps of this problem for several work splits -- the FP32c particle
+    block (particles a unit sums for together) and the units of design x particle block x
+    segment chunk per CTA --, keep the fastest for later tracking calls of the process and
+    return its units per CTA (cct_autotune; `particle_block()` gives its particle block)."""
     lib = _lib.load()
     dev = ds.kls.device
     p = torch.as_tensor(np.asarray(particles, dtype=np.float64) if not isinstance(particles, torch.Tensor)
@@ -542,3 +543,14 @@ def autotune(ds: DesignSet, particles, footstep: float, precision: str = "f32c",
 def set_units_per_cta(n: int = 0) -> None:
     """Set the tracking work split by hand (0 restores the default of 8)."""
     _lib.check(_lib.load().cct_track_set_units_per_cta(int(n)), "cct_track_set_units_per_cta")
+
+
+def set_particle_block(n: int = 0) -> None:
+    """Set the FP32c particle block by hand: 32, 64, 128 or 256 (0 restores the automatic
+    choice)."""
+    _lib.check(_lib.load().cct_track_set_particle_block(int(n)), "cct_track_set_particle_block")
+
+
+def particle_block() -> int:
+    """The process-wide FP32c particle block (0: automatic)."""
+    return int(_lib.load().cct_track_particle_block())

@@ -161,16 +161,26 @@ int cct_track_async(const double *d_kls, const double *d_p0s,
                     void *d_scratch, int64_t scratch_bytes, void *stream);
 int cct_track_status(const void *d_scratch, void *stream);
 
-/* Work split of the tracking kernels: units of (design, particle block,
- * segment chunk) per CTA and RK4 stage (default 8; 1..64, 0 restores the
- * default).  Process-wide.  cct_autotune times a few RK4 steps of the caller's
- * problem (`steps` steps of `footstep`, on a copy of d_particles, which is not
- * modified) for 2, 4, 8, 16 and 32 units per CTA, keeps the fastest and
- * returns it; it needs cct_autotune_scratch_bytes() of scratch.  Stands in for
- * the reference's block_dim_x choice (GPU_ACCELERATOR(block_dim_x=...),
+/* Work split of the tracking kernels, process-wide:
+ *  - units of (design, particle block, segment chunk) per CTA and RK4 stage
+ *    (default 8; 1..64, 0 restores the default);
+ *  - the FP32c particle block: particles whose field sums a unit computes
+ *    together (32, 64, 128 or 256; 0 = automatic, the power of two that needs
+ *    the fewest particle slots, the largest of those).  FP64 tracking always
+ *    uses blocks of 32, and cct_track_adjoint the automatic choice.
+ * cct_autotune times a few RK4 steps of the caller's problem (`steps` steps of
+ * `footstep`, on a copy of d_particles, which is not modified) for every
+ * particle block from the automatic one up to the first that holds all of a
+ * design's particles (FP32c) and 2, 4, 8, 16 and 32 units per CTA, keeps the
+ * fastest pair as the process-wide setting and returns its units per CTA
+ * (cct_track_particle_block() then gives its particle block); it needs
+ * cct_autotune_scratch_bytes() of scratch.  Stands in for the reference's
+ * block_dim_x choice (GPU_ACCELERATOR(block_dim_x=...),
  * gpu_accelerator.py:54-96), which the caller sets by hand.  Synchronous. */
 int cct_track_set_units_per_cta(int32_t units_per_cta);
 int32_t cct_track_units_per_cta(void);
+int cct_track_set_particle_block(int32_t particles);
+int32_t cct_track_particle_block(void);
 int64_t cct_autotune_scratch_bytes(int32_t n_designs, int64_t n_particles);
 int cct_autotune(const double *d_kls, const double *d_p0s,
                  const int64_t *d_seg_off, const void *d_packed,
@@ -213,17 +223,27 @@ int cct_track_adjoint(const double *d_kls, const double *d_p0s,
  * device memory once running (memory reserved up front by a host application;
  * a C caller that owns only the buffers it passes).  No counterpart in the
  * reference: cctpy's GPU path allocates and copies on every call.  The scratch
- * is a fixed device array inside the library, created on each GPU when the
- * library is loaded and held until the process exits; its size,
- * cct_track_static_scratch_bytes() = 32 MiB, bounds the problem (for example
- * 64 designs x 512 protons, or one design x 100 000 protons), and at most 64
- * designs are taken.  Larger problems return CCT_ERR_ARG with the size they
- * need; use cct_track with a caller buffer for them.  The first call on a
- * device looks up the array's address on that device; make that first call
- * before any stream capture.  Every call shares the array: calls whose kernels
- * overlap on the GPU (other streams, other host threads) race and must be
- * serialised by the caller.  Same arguments, results and status codes as
- * cct_track otherwise; no cudaMalloc/cudaFree is made. */
+ * is a fixed device array inside the library, held on each GPU until the
+ * process exits; its size, cct_track_static_scratch_bytes() = 32 MiB, bounds
+ * the problem (for example 64 designs x 512 protons, or one design x 100 000
+ * protons), and at most 64 designs are taken.  Larger problems return
+ * CCT_ERR_ARG with the size they need; use cct_track with a caller buffer for
+ * them.
+ * The array takes its device memory when the CUDA module holding it is loaded
+ * on a device, which under lazy module loading (the CUDA default) is its first
+ * use there, not the loading of the library.  Place it at start-up, before the
+ * application reserves its memory: call cct_track_static_scratch_bytes() with
+ * each device current once (with a device visible it looks the array up on the
+ * current device, which loads the module), or make the first
+ * cct_track_static_scratch call on each device then.  That first lookup on a
+ * device records the array's address for the life of the process; make it
+ * before any stream capture, and do not use this entry point on a device
+ * after cudaDeviceReset on it.  Every call shares the array: calls whose
+ * kernels overlap on the GPU (other streams, other host threads) race and must
+ * be serialised by the caller.  Synchronous: like cct_track it reads the
+ * segment offsets back and waits for `stream` before returning.  Same
+ * arguments, results and status codes as cct_track otherwise; no
+ * cudaMalloc/cudaFree is made. */
 int64_t cct_track_static_scratch_bytes(void);
 int cct_track_static_scratch(const double *d_kls, const double *d_p0s,
                              const int64_t *d_seg_off, const void *d_packed,

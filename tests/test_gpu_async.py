@@ -71,8 +71,32 @@ def test_autotune_picks_a_split_and_keeps_results(population):
         best = engine.autotune(ds, ps, 0.01, "f64", steps=2)
         assert best in (2, 4, 8, 16, 32)
         assert engine._lib.load().cct_track_units_per_cta() == best
+        assert engine.particle_block() == 0            # FP64 keeps blocks of 32
         tuned = engine.track(ds, ps, 0.05, 0.01, "f64")
         assert np.abs(tuned[..., 0:3] - base[..., 0:3]).max() <= 1e-12
     finally:
         engine.set_units_per_cta(0)
     assert engine._lib.load().cct_track_units_per_cta() == 8
+
+
+def test_autotune_particle_block_f32c(population):
+    """FP32c: the autotuner also picks the particle block (40 protons a design: the automatic
+    block of 64, or 32); every split it may keep gives the same tracks to FP32 rounding of a
+    different chunk split."""
+    ds, ps = population
+    base = engine.track(ds, ps, 0.05, 0.01, "f32c")
+    try:
+        best = engine.autotune(ds, ps, 0.01, "f32c", steps=2)
+        assert best in (2, 4, 8, 16, 32)
+        assert engine.particle_block() in (0, 32, 64)
+        tuned = engine.track(ds, ps, 0.05, 0.01, "f32c")
+        assert np.abs(tuned[..., 0:3] - base[..., 0:3]).max() <= 1e-8
+        for g in (32, 64, 128):
+            engine.set_particle_block(g)
+            out = engine.track(ds, ps, 0.05, 0.01, "f32c")
+            assert np.abs(out[..., 0:3] - base[..., 0:3]).max() <= 1e-8
+            assert np.array_equal(out[..., 6:], base[..., 6:])
+    finally:
+        engine.set_units_per_cta(0)
+        engine.set_particle_block(0)
+    assert engine.particle_block() == 0

@@ -143,3 +143,30 @@ def test_bad_arguments(lib):
     assert lib.cct_test_plan_units(p(ok), 1, 10, 2, 456, 0, p(t), p(t), p(t), ctypes.byref(g)) == -2
     assert lib.cct_test_plan_units(p(ok), 1, 0, 1, 456, 0, p(t), p(t), p(t), ctypes.byref(g)) == -2
     assert lib.cct_test_plan_units(p(ok), 1, 10, 1, 0, 0, p(t), p(t), p(t), ctypes.byref(g)) == -2
+
+
+def test_particle_block_setting(lib):
+    """The FP32c particle block set by hand (or by cct_autotune) is the one the planner uses;
+    FP64 keeps blocks of 32; 0 restores the automatic choice; other sizes are refused."""
+    try:
+        assert lib.cct_track_particle_block() == 0
+        assert plan(lib, [46080], 4096, 1, 456)[4] == 256
+        for g in (32, 64, 128, 256):
+            assert lib.cct_track_set_particle_block(g) == _lib.CCT_OK
+            assert lib.cct_track_particle_block() == g
+            units, unit_off, chunks, ct, got = plan(lib, [46080, 12345], 4096, 1, 456)
+            assert got == g
+            assert units == unit_off[-1] and np.all(unit_off[1:] - unit_off[:-1] == (4096 // g) * chunks)
+            assert plan(lib, [46080], 4096, 0, 456)[4] == 32
+        for bad in (-1, 16, 48, 512):
+            assert lib.cct_track_set_particle_block(bad) == _lib.CCT_ERR_ARG
+        assert lib.cct_track_particle_block() == 256          # a refused value leaves the setting alone
+        # every split the autotuner tries fits the scratch it asks for
+        need = lib.cct_autotune_scratch_bytes(1, 4096)
+        for g in (32, 64, 128, 256):
+            lib.cct_track_set_particle_block(g)
+            assert need >= lib.cct_track_scratch_bytes(1, 4096) + 80 * 4096
+    finally:
+        lib.cct_track_set_particle_block(0)
+    assert lib.cct_track_particle_block() == 0
+    assert plan(lib, [46080], 100, 1, 456)[4] == 128

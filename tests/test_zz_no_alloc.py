@@ -50,21 +50,58 @@ def test_static_scratch_matches_caller_scratch_twice(precision):
 
 
 def test_static_scratch_refuses_oversized_problems():
+    """Every refused call is given buffers of the sizes it declares, so that even a
+    regressed size check could not read or write past them."""
     lib = _lib.load()
     assert lib.cct_track_static_scratch_bytes() == 32 << 20
     _, cct = W.build_single_dipole()
     ds = engine.design_of(cct)
-    ps = torch.as_tensor(W.single_dipole_particles(2, 0)).cuda().contiguous()
     stream = torch.cuda.current_stream().cuda_stream
-    # more particles than the array can hold state for: refused before any launch
+    # 200 000 particles: their records take 16 MB, their RK4 state alone 38 MB, more than the
+    # 32 MiB array holds -- refused before any launch, the records untouched
+    n_big = 200_000
+    big = torch.as_tensor(np.tile(W.single_dipole_particles(2, 0), (n_big // 2, 1))).cuda().contiguous()
+    before = big.clone()
     rc = lib.cct_track_static_scratch(ds.kls.data_ptr(), ds.p0s.data_ptr(), ds.seg_off.data_ptr(), 0, 0,
-                                      ds.qs_off.data_ptr(), 1, ps.data_ptr(), 1 << 22, 0.01, 0.001, 0, stream)
+                                      ds.qs_off.data_ptr(), 1, big.data_ptr(), n_big, 0.01, 0.001, 0, stream)
     assert rc == _lib.CCT_ERR_ARG
     assert "static scratch holds" in _lib.last_error()
-    # more designs than the entry point takes
-    rc = lib.cct_track_static_scratch(ds.kls.data_ptr(), ds.p0s.data_ptr(), ds.seg_off.data_ptr(), 0, 0,
-                                      ds.qs_off.data_ptr(), 65, ps.data_ptr(), 2, 0.01, 0.001, 0, stream)
+    assert torch.equal(big, before)
+    # 65 designs (one more than the entry point takes), with offsets and records for all of them
+    n_d = 65
+    seg_off = torch.zeros(n_d + 1, dtype=torch.int64, device="cuda")
+    qs_off = torch.zeros(n_d + 1, dtype=torch.int64, device="cuda")
+    many = torch.as_tensor(np.tile(W.single_dipole_particles(2, 0), (n_d, 1))).cuda().contiguous()
+    rc = lib.cct_track_static_scratch(ds.kls.data_ptr(), ds.p0s.data_ptr(), seg_off.data_ptr(), 0, 0,
+                                      qs_off.data_ptr(), n_d, many.data_ptr(), 2, 0.01, 0.001, 0, stream)
     assert rc == _lib.CCT_ERR_ARG
     # the refusals left the device usable
-    out = static_track(ds, ps.cpu().numpy(), 0.01, 0.001, "f64")
+    out = static_track(ds, W.single_dipole_particles(2, 0), 0.01, 0.001, "f64")
     assert np.isfinite(out).all()
+
+
+@pytest.mark.parametrize("precision", ["f64", "f32c"])
+def test_static_scratch_call_takes_no_device_memory(precision):
+    """The defining property: with its inputs in place, a call changes the device's free
+    memory by nothing (no cudaMalloc, no library allocation behind it)."""
+    lib = _lib.load()
+    _, cct = W.build_single_dipole()
+    ds = engine.design_of(cct)
+    packed = ds.packed().data_ptr() if precision == "f32c" else 0
+    p = torch.as_tensor(W.single_dipole_particles(64, 3)).cuda().contiguous()
+    stream = torch.cuda.current_stream().cuda_stream
+
+    def call():
+        rc = lib.cct_track_static_scratch(ds.kls.data_ptr(), ds.p0s.data_ptr(), ds.seg_off.data_ptr(), packed, 0,
+                                          ds.qs_off.data_ptr(), 1, p.data_ptr(), p.shape[0], 0.02, 0.001,
+                                          PREC[precision], stream)
+        _lib.check(rc, "cct_track_static_scratch")
+
+    call()                                  # first call: module, kernel and array already placed
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    call()
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0
+    assert torch.isfinite(p).all()
