@@ -101,22 +101,48 @@ class ClockSampler:
 
 
 # ---------------------------------------------------------------- CPU oracle (reference arm / cpu_baseline)
-def oracle_field_sample(n_points: int, seed: int, processes: int):
-    """Time the CPU oracle (numpy restatement of cctpy's CCT.magnetic_field_at, over a spawn
-    process pool on all cores) on n_points points of the same workload.  Returns pairs/s."""
+def oracle_single_dipole():
+    """The oracle's record of the single dipole (the field-map and C0 magnet)."""
     from oracle import cct_oracle as O
     from cctpy_gb300 import workloads as W
     c = W.SINGLE_DIPOLE
     orb = O.Orbit((0.0, 0.0), (1.0, 0.0), c["drift"]).add_arc(c["big_r"], c["clockwise"], c["bending_angle"])
-    rec = O.cct_along(orb, c["drift"], c["big_r"], c["small_r"], c["bending_angle"], c["tilt_angles"],
-                      c["winding_number"], c["current"], (0.0, 0.0),
-                      (2 * math.pi * c["winding_number"], O.deg2rad(-c["bending_angle"])),
-                      c["disperse_number_per_winding"])
+    return O.cct_along(orb, c["drift"], c["big_r"], c["small_r"], c["bending_angle"], c["tilt_angles"],
+                       c["winding_number"], c["current"], (0.0, 0.0),
+                       (2 * math.pi * c["winding_number"], O.deg2rad(-c["bending_angle"])),
+                       c["disperse_number_per_winding"])
+
+
+def oracle_pool(processes: int):
+    """Spawn-started pool of oracle workers holding the single dipole, built once: the timed
+    CPU legs then measure field sums and RK4 steps, not pool start-up."""
+    from oracle import cct_oracle as O
+    return O.OraclePool([oracle_single_dipole()], processes)
+
+
+def oracle_field_sample(pool, n_points: int, seed: int):
+    """Time the CPU oracle (numpy restatement of cctpy's CCT.magnetic_field_at) over the pool on
+    n_points points of the field-map workload.  Returns (pairs/s, seconds, points, fields)."""
+    from cctpy_gb300 import workloads as W
     pts = W.field_map_points(n_points, seed=seed)
     t0 = time.perf_counter()
-    O.field_many([rec], pts, processes=processes)
+    B = pool.field(pts)
     dt = time.perf_counter() - t0
-    return n_points * N_SEG / dt, dt
+    return n_points * N_SEG / dt, dt, pts, B
+
+
+def oracle_track_sample(pool, n_protons: int):
+    """Time the oracle's RK4 track (cctpy's ParticleRunner.run_only path: particles.py:562-596
+    with the RK4 of base_utils.py:264-311) of n_protons C0 protons through the whole single-dipole
+    arc at 1 mm, one proton per worker.  Returns (particle-steps/s, seconds, steps, inputs, outputs)."""
+    from cctpy_gb300 import workloads as W
+    ps = W.single_dipole_particles(n_protons, seed=0)
+    L = W.single_dipole_track_length()
+    steps = int(np.ceil(L / 0.001))
+    t0 = time.perf_counter()
+    out = pool.track(ps, L, 0.001)
+    dt = time.perf_counter() - t0
+    return n_protons * steps / dt, dt, steps, ps, out
 
 
 def run_reference(args):
@@ -125,13 +151,12 @@ def run_reference(args):
         return
     cores = os.cpu_count() or 1
     n = args.ref_points
-    for k in range(max(args.warmup, 0)):   # untimed: a small sample each (pool start-up, page-in)
-        oracle_field_sample(max(cores * 4, 64), seed=100 + k, processes=cores)
-    rates, times = [], []
-    for k in range(args.steps):
-        r, dt = oracle_field_sample(n, seed=200 + k, processes=cores)
-        rates.append(r)
-        times.append(dt)
+    with oracle_pool(cores) as pool:
+        for k in range(max(args.warmup, 0)):   # untimed: workers page in numpy and the segments
+            oracle_field_sample(pool, max(cores * 4, 64), seed=100 + k)
+        times = []
+        for k in range(args.steps):
+            times.append(oracle_field_sample(pool, n, seed=200 + k)[1])
     value = (n * N_SEG * args.steps) / sum(times) / 1e9
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "Gpairs/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / args.steps,
@@ -139,22 +164,24 @@ def run_reference(args):
             "config": {"workload": WORKLOAD, "n_points_per_step": n, "n_segments": N_SEG,
                        "sample": f"{n} of the 2^20 field points per step"},
             "cpu_baseline": {"value": value, "unit": "Gpairs/s", "cores": cores, "kind": "port",
-                             "sample": f"{n} points x {N_SEG} segments per step, {args.steps} steps"},
+                             "sample": f"{n} points x {N_SEG} segments per step, {args.steps} steps, over a "
+                                       f"{cores}-process pool started and warmed before the timed steps"},
             "e2e": {"value": value, "unit": "Gpairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
 
 # ---------------------------------------------------------------- tracking (beside the headline)
 def measure_tracking(args, dev, rank):
-    """RK4 tracking throughput, FP32c vs FP64, on a slice of the tracking workloads:
-    the gantry section (597 600 segments, 4096 protons, 1 mm steps) and a design population
-    (64 second-section designs of uneven segment counts, 512 protons each, one launch).
-    Per-step cost does not depend on the track length, so a few steps stand for the 3.5 m
-    track.  Returns a dict of particle-steps/s and Gpairs/s."""
+    """RK4 tracking throughput, FP32c vs FP64, over equal windows (same steps, same
+    repetitions, best of them): C0 whole, and slices of C2 (the gantry section: 597 600
+    segments, 4096 protons, 1 mm steps) and C3 (64 second-section designs of uneven segment
+    counts, 512 protons each, one launch; also through cct_track_async captured once in a CUDA
+    graph and replayed).  The cost of a step does not depend on the track length, so a few
+    steps stand for the 3.5 m track.  Returns a dict of particle-steps/s and Gpairs/s."""
     import torch
     from cctpy_gb300 import HUST_SC_GANTRY, engine, workloads as W
 
-    def timed(ds, ps, steps, prec, reps=2):
+    def timed(ds, ps, steps, prec, reps):
         engine.track(ds, ps, 0.002, 0.001, prec)          # warm-up (2 steps)
         torch.cuda.synchronize()
         best = float("inf")
@@ -165,7 +192,21 @@ def measure_tracking(args, dev, rank):
             best = min(best, time.perf_counter() - t0)
         return best
 
-    out = {}
+    def tuned(ds_, ps_, steps, n_p, reps):
+        """The same FP32c slice after cct_autotune picked the work split for this problem."""
+        best = engine.autotune(ds_, ps_, 0.001, "f32c", steps=2)
+        block = engine.particle_block()
+        try:
+            t = timed(ds_, ps_, steps, "f32c", reps)
+        finally:
+            engine.set_units_per_cta(0)
+            engine.set_particle_block(0)
+        r = ds_.n_designs * n_p * steps / t
+        return {"units_per_cta": best, "particle_block": block or "automatic", "seconds": t,
+                "particle_steps_per_s": r, "gpairs_per_s": n_p * steps * 4 * ds_.n_segments / t / 1e9}
+
+    out = {"windows": "FP32c and FP64 timed over the same RK4 steps and repetitions (best of them), "
+                      "each call with its host copies of the particle records"}
     # C0: the reference's CPU-runnable case, whole track (32 protons, 374 steps of 1 mm)
     _, dip = W.build_single_dipole()
     dsd = engine.design_of(dip)
@@ -177,62 +218,54 @@ def measure_tracking(args, dev, rank):
     for prec in ("f32c", "f64"):
         engine.track(dsd, p32, 0.002, 0.001, prec)
         torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        engine.track(dsd, p32, L0, 0.001, prec)
-        torch.cuda.synchronize()
-        t = time.perf_counter() - t0
-        c0[prec] = {"seconds": t, "steps": n0, "us_per_stage": t / (4 * n0) * 1e6,
-                    "gpairs_per_s": 32 * n0 * 4 * dsd.n_segments / t / 1e9}
+        best = float("inf")
+        for _ in range(2):
+            t0 = time.perf_counter()
+            engine.track(dsd, p32, L0, 0.001, prec)
+            torch.cuda.synchronize()
+            best = min(best, time.perf_counter() - t0)
+        c0[prec] = {"seconds": best, "steps": n0, "us_per_stage": best / (4 * n0) * 1e6,
+                    "particle_steps_per_s": 32 * n0 / best, "gpairs_per_s": 32 * n0 * 4 * dsd.n_segments / best / 1e9}
     out["single_dipole"] = dict(
         workload=f"single CCT dipole, {dsd.n_segments} segments; 32 protons 250 MeV through the whole "
-                 f"{L0:.4f} m arc at 1 mm ({n0} RK4 steps), one call (latency-bound: 1 particle block)", **c0)
+                 f"{L0:.4f} m arc at 1 mm ({n0} RK4 steps), one call, best of 2 (latency-bound: one particle block)",
+        speedup_f32c_vs_f64=c0["f64"]["seconds"] / c0["f32c"]["seconds"], **c0)
     bl = W.build_gantry_section()
     ds = engine.design_of(bl)
     ds.packed()
     ps = W.beam_particles(bl, 4096, seed=2 + rank, kinetic_MeV=215.0)
     n_seg = ds.n_segments
-    s32, s64 = args.track_steps, max(1, args.track_steps // 10)
-    t32 = timed(ds, ps, s32, "f32c")
-    t64 = timed(ds, ps, s64, "f64", reps=1)
-    r32, r64 = 4096 * s32 / t32, 4096 * s64 / t64
-    out["gantry_section"] = {
-        "workload": f"HUST second section, AG tilts [90,30,90,90], -7000 A, {n_seg} segments + 1 QS; 4096 protons "
-                    "215 MeV, 1 mm RK4 steps (one cooperative launch per call, host copies included)",
-        "f32c": {"steps": s32, "seconds": t32, "particle_steps_per_s": r32, "gpairs_per_s": r32 * 4 * n_seg / 1e9},
-        "f64": {"steps": s64, "seconds": t64, "particle_steps_per_s": r64, "gpairs_per_s": r64 * 4 * n_seg / 1e9},
-        "speedup_f32c_vs_f64": r32 / r64}
-
-    def tuned(ds_, ps_, steps, n_p):
-        """The same FP32c slice after cct_autotune picked the work split for this problem."""
-        best = engine.autotune(ds_, ps_, 0.001, "f32c", steps=2)
-        try:
-            t = timed(ds_, ps_, steps, "f32c")
-        finally:
-            engine.set_units_per_cta(0)
-        r = ds_.n_designs * n_p * steps / t
-        return {"units_per_cta": best, "seconds": t, "particle_steps_per_s": r,
-                "gpairs_per_s": n_p * steps * 4 * ds_.n_segments / t / 1e9}
-
-    out["gantry_section"]["f32c_autotuned"] = tuned(ds, ps, s32, 4096)
+    steps, reps = args.track_steps, 2
+    res = {}
+    for prec in ("f32c", "f64"):
+        t = timed(ds, ps, steps, prec, reps)
+        r = 4096 * steps / t
+        res[prec] = {"steps": steps, "reps": reps, "seconds": t, "particle_steps_per_s": r,
+                     "gpairs_per_s": r * 4 * n_seg / 1e9}
+    out["gantry_section"] = dict(
+        workload=f"HUST second section, AG tilts [90,30,90,90], -7000 A, {n_seg} segments + 1 QS; 4096 protons "
+                 "215 MeV, 1 mm RK4 steps (one cooperative launch per call, host copies included)",
+        speedup_f32c_vs_f64=res["f32c"]["particle_steps_per_s"] / res["f64"]["particle_steps_per_s"], **res)
+    out["gantry_section"]["f32c_autotuned"] = tuned(ds, ps, steps, 4096, reps)
     if not args.no_population:
         bls = [HUST_SC_GANTRY(**kw).create_second_bending_part_beamline() for kw in W.design_population(64, seed=3)]
         dsp = engine.design_set_of(bls)
         dsp.packed()
         pp = W.beam_particles(bls[0], 512, seed=2 + rank, kinetic_MeV=215.0)
-        tp = timed(dsp, pp, s32 // 2, "f32c", reps=1)
-        rp = 64 * 512 * (s32 // 2) / tp
-        tp64 = timed(dsp, pp, 1, "f64", reps=1)
-        rp64 = 64 * 512 / tp64
+        psteps = max(1, steps // 2)
+        res = {}
+        for prec in ("f32c", "f64"):
+            t = timed(dsp, pp, psteps, prec, reps)
+            r = 64 * 512 * psteps / t
+            res[prec] = {"steps": psteps, "reps": reps, "seconds": t, "particle_steps_per_s": r,
+                         "gpairs_per_s": 512 * psteps * 4 * dsp.n_segments / t / 1e9}
         segs = [dsp.segments_of(d) for d in range(64)]
-        out["design_population"] = {
-            "workload": f"64 designs ({min(segs)}..{max(segs)} segments, {dsp.n_segments} total), 512 protons each, "
-                        "one launch",
-            "f32c": {"steps": s32 // 2, "seconds": tp, "particle_steps_per_s": rp,
-                     "gpairs_per_s": 512 * (s32 // 2) * 4 * dsp.n_segments / tp / 1e9},
-            "f64": {"steps": 1, "seconds": tp64, "particle_steps_per_s": rp64,
-                    "gpairs_per_s": 512 * 4 * dsp.n_segments / tp64 / 1e9},
-            "speedup_f32c_vs_f64": rp / rp64,
-            "f32c_autotuned": tuned(dsp, pp, s32 // 2, 512)}
+        out["design_population"] = dict(
+            workload=f"64 designs ({min(segs)}..{max(segs)} segments, {dsp.n_segments} total), 512 protons each, "
+                     "one launch",
+            speedup_f32c_vs_f64=res["f32c"]["particle_steps_per_s"] / res["f64"]["particle_steps_per_s"], **res)
+        out["design_population"]["f32c_graph_replay"] = measure_graph_replay(dsp, pp, psteps)
+        out["design_population"]["f32c_autotuned"] = tuned(dsp, pp, psteps, 512, reps)
     if not args.no_speed_test:
         out["reference_speed_test"] = measure_speed_test(rank)
     if not args.no_adjoint:
@@ -240,6 +273,49 @@ def measure_tracking(args, dev, rank):
     if not args.no_generation:
         out["optimiser_generation"] = measure_generation(args, rank)
     return out
+
+
+def measure_graph_replay(ds, ps, steps, replays=5):
+    """C3 as configured: the population's FP32c tracking enqueued by cct_track_async (plan kernel
+    + cooperative tracking launch, no host read-back), captured once in a CUDA graph and
+    replayed; each replay first restores the start records (device copy, in the graph).  Timed
+    with CUDA events over the replays, beside the same launch enqueued directly; both
+    device-resident (the synchronous engine.track line above includes its host copies)."""
+    import torch
+    from cctpy_gb300 import engine
+    n_p = ps.shape[0]
+    start = torch.as_tensor(np.broadcast_to(ps, (ds.n_designs,) + ps.shape).copy(), device="cuda")
+    p = start.clone()
+    tl = engine.TrackLaunch(ds, p, steps * 0.001, 0.001, "f32c")
+    tl.launch()                       # first call outside any capture (occupancy query)
+    tl.status()
+    direct = None
+    for _ in range(2):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(replays):
+            p.copy_(start)
+            tl.launch()
+        e1.record()
+        tl.status()
+        direct = e0.elapsed_time(e1) / replays / 1e3
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        p.copy_(start)
+        tl.launch()
+    g.replay()
+    tl.status()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(replays):
+        g.replay()
+    e1.record()
+    tl.status()
+    t = e0.elapsed_time(e1) / replays / 1e3
+    r = ds.n_designs * n_p * steps / t
+    return {"steps": steps, "replays": replays, "seconds_per_replay": t, "particle_steps_per_s": r,
+            "gpairs_per_s": n_p * steps * 4 * ds.n_segments / t / 1e9, "seconds_per_direct_launch": direct,
+            "call": "engine.TrackLaunch (cct_track_async) captured by torch.cuda.graph, device-resident"}
 
 
 def measure_speed_test(rank):
@@ -350,13 +426,16 @@ def measure_generation(args, rank):
 
 
 def measure_design_grads(args, rank):
-    """design-grads/s: 13-parameter gradients of J = <x^2> + <y^2> at the exit for 16 gantry
-    designs x 1024 protons in one adjoint run, on a slice of RK4 steps (1 mm):
-    FP32c (forward and adjoint sweeps in packed FP32 with compensation) on args.adjoint_steps
-    steps, the FP64 adjoint on 1/16 of them.  Timed apart: the design set (segments generated
-    on the GPU from layer records), the adjoint (cct_track_adjoint: forward with checkpoints,
-    recompute, reverse sweeps, segment gradients) and the parameter Jacobian (forward-mode
-    contraction on the GPU, cct_segments_param_grad, plus the 13-parameter grouping)."""
+    """C4: 13-parameter gradients of J = <x^2> + <y^2> at the exit for 16 gantry designs x 1024
+    protons in one adjoint run (1 mm RK4 steps), with the configuration's RK4 checkpointing
+    every 64 steps and recompute: the forward keeps a checkpoint every 64 steps, and each
+    segment is recomputed (its stage records written) before its reverse sweep.  FP32c
+    (forward and adjoint sweeps in packed FP32 with compensation) on args.adjoint_steps steps,
+    the FP64 adjoint on args.adjoint_steps_f64 of them.  Timed apart: the design set (segments
+    generated on the GPU from layer records), the adjoint (cct_track_adjoint) and the parameter
+    Jacobian (forward-mode contraction on the GPU, cct_segments_param_grad, plus the
+    13-parameter grouping).  A design-grad-step is one RK4 step of one design's gradient; a
+    whole C4 gradient over the 3.5 m track at 1 mm is 3500 of them."""
     import torch
     from cctpy_gb300 import engine, workloads as W
     from cctpy_gb300.adjoint import GantryDesign, exit_frame, layer_grads_from_rows, segment_gradient
@@ -375,17 +454,19 @@ def measure_design_grads(args, rank):
     torch.cuda.synchronize()
     t_setup = time.perf_counter() - t0
     n_seg = ds.n_segments
+    full_steps = 3500
     out = {"workload": f"16 second-section designs ({n_seg} segments total), 1024 protons each, 13 parameters "
-                       "(8 tilts, 4 layer currents, winding radius), J = <x^2>+<y^2> at the exit; "
-                       "stage records of the whole slice kept in HBM (one checkpoint segment, no recompute)",
-           "design_set_seconds": t_setup}
-    for prec, steps in (("f32c", args.adjoint_steps), ("f64", max(1, args.adjoint_steps // 16))):
+                       "(8 tilts, 4 layer currents, winding radius), J = <x^2>+<y^2> at the exit; 1 mm RK4 steps, "
+                       "checkpoint every 64 steps with recompute",
+           "design_set_seconds": t_setup, "full_track_steps": full_steps}
+    for prec, steps in (("f32c", args.adjoint_steps), ("f64", args.adjoint_steps_f64)):
         L = steps * 0.001
+        ck = min(64, steps)
         frames = np.tile(exit_frame(designs[0].beamline.trajectory, L, 215.0), (16, 1))
-        segment_gradient(ds, ps, 0.002, 0.001, frames, None, prec)        # warm-up
+        segment_gradient(ds, ps, 0.002, 0.001, frames, 2, prec)        # warm-up
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        J, seg, _ = segment_gradient(ds, ps, L, 0.001, frames, None, prec, on_device=True)
+        J, seg, _ = segment_gradient(ds, ps, L, 0.001, frames, ck, prec, on_device=True)
         torch.cuda.synchronize()
         t_gpu = time.perf_counter() - t0
         t0 = time.perf_counter()
@@ -393,15 +474,55 @@ def measure_design_grads(args, rank):
         g = [d.gradient(layer_grads_from_rows(d.beamline.magnets, rows[ds.layer_design == i]))
              for i, d in enumerate(designs)]
         t_jac = time.perf_counter() - t0
-        fwd_pairs = 1024 * steps * 4 * n_seg
-        out[prec] = {"steps": steps, "adjoint_seconds": t_gpu, "jacobian_seconds": t_jac,
-                     "design_grads_per_s": 16 / (t_gpu + t_jac),
-                     "design_grad_steps_per_s": 16 * steps / (t_gpu + t_jac),
+        fwd_pairs = 1024 * steps * 4 * n_seg          # each design's protons x its own segments
+        rate = 16 * steps / (t_gpu + t_jac)
+        out[prec] = {"steps": steps, "checkpoint_steps": ck, "checkpoint_segments": -(-steps // ck),
+                     "adjoint_seconds": t_gpu, "jacobian_seconds": t_jac,
+                     "design_grad_steps_per_s": rate,
                      "design_grad_steps_per_s_adjoint": 16 * steps / t_gpu,
+                     "full_track_design_grads_per_s": rate / full_steps,
+                     "seconds_per_16_full_track_gradients": 16 * full_steps / rate,
                      "forward_equivalent_gpairs_per_s": fwd_pairs / t_gpu / 1e9,
                      "gradient_norm_design0": float(np.linalg.norm(g[0]))}
     out["speedup_f32c_vs_f64"] = out["f32c"]["design_grad_steps_per_s"] / out["f64"]["design_grad_steps_per_s"]
     return out
+
+
+# ---------------------------------------------------------------- CPU baselines beside the GPU arm
+def measure_cpu_baselines(args, ds):
+    """The oracle on the machine's host cores (rank 0, one GPU): field sums on args.cpu_points of the
+    field-map points, and the C0 track (as many 250 MeV protons as cores, the whole 374-step
+    arc at 1 mm).  Both GPU forms are compared with the oracle on the same inputs (C1's
+    "max and RMS relative |B| error vs the FP64 CPU oracle"; final positions of C0)."""
+    import torch
+    from cctpy_gb300 import engine, workloads as W
+    cores = os.cpu_count() or 1
+    with oracle_pool(cores) as pool:
+        oracle_field_sample(pool, cores * 4, seed=299)                    # workers ready (untimed)
+        rate, dt, pts, B_cpu = oracle_field_sample(pool, args.cpu_points, seed=300)
+        cpu = {"value": rate / 1e9, "unit": "Gpairs/s", "cores": cores, "kind": "port",
+               "sample": f"{args.cpu_points} of the 2^20 points x {N_SEG} segments ({dt:.1f} s, numpy oracle over a "
+                         f"{cores}-process pool started and warmed before the timed call)"}
+        acc = {"points": int(args.cpu_points)}
+        for prec in ("f64", "f32c"):
+            B = engine.field_at_points(ds, pts, prec)
+            rel = np.linalg.norm(B - B_cpu, axis=1) / np.linalg.norm(B_cpu, axis=1)
+            acc[f"max_rel_{prec}_vs_oracle"] = float(rel.max())
+            acc[f"rms_rel_{prec}_vs_oracle"] = float(np.sqrt(np.mean(rel ** 2)))
+        cpu_track = None
+        if not args.no_tracking:
+            trate, tdt, steps, p_in, p_out = oracle_track_sample(pool, cores)
+            L = W.single_dipole_track_length()
+            dev = {}
+            for prec in ("f64", "f32c"):
+                got = engine.track(ds, p_in, L, 0.001, prec)[0]
+                dev[f"max_pos_diff_m_{prec}"] = float(np.abs(got[:, 0:3] - p_out[:, 0:3]).max())
+            torch.cuda.synchronize()
+            cpu_track = {"value": trate, "unit": "particle-steps/s", "cores": cores, "kind": "port",
+                         "sample": f"{cores} C0 protons (250 MeV, one per process) through the whole {L:.4f} m "
+                                   f"single-dipole arc at 1 mm ({steps} RK4 steps, {N_SEG} segments): {tdt:.1f} s",
+                         "gpairs_per_s": trate * 4 * N_SEG / 1e9, "gpu_vs_cpu_final_position": dev}
+    return cpu, cpu_track, acc
 
 
 # ---------------------------------------------------------------- GPU arm
@@ -530,14 +651,9 @@ def run_ours(args):
 
     line = None
     if rank == 0:
-        cpu = None
+        cpu = cpu_track = acc_oracle = None
         if world == 1 and not args.no_cpu_baseline:
-            cores = os.cpu_count() or 1
-            n = args.cpu_points
-            rate, dt = oracle_field_sample(n, seed=300, processes=cores)
-            cpu = {"value": rate / 1e9, "unit": "Gpairs/s", "cores": cores, "kind": "port",
-                   "sample": f"{n} of the 2^20 points x {N_SEG} segments ({dt:.1f} s, numpy oracle over a "
-                             f"{cores}-process spawn pool)"}
+            cpu, cpu_track, acc_oracle = measure_cpu_baselines(args, ds)
         line = {
             "metric": METRIC, "value": value, "unit": "Gpairs/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
@@ -557,7 +673,10 @@ def run_ours(args):
                          "traffic_unit": "bytes per launch (dram read + write, from an ncu capture of this kernel "
                                          "on this workload)",
                          "peak_source": "measured in this run: best of scalar FFMA and packed FP32x2 FMA "
-                                        "chains (cct_probe_fma_peak)",
+                                        "chains (cct_probe_fma_peak); the driver's measured peaks hold no FP32 or "
+                                        "FP64 CUDA-core figure, and its bf16 tensor and HBM peaks do not bound "
+                                        "this non-contraction",
+                         "frac_of": "measured FP32 FMA-pipe peak (this run's probe)",
                          "peak_scalar_ffma": peak32_scalar, "peak_packed_ffma2": peak32_packed,
                          "flops_per_pair": FLOPS_PER_PAIR, "kernel": "field_f32c_kernel",
                          "kernel_ms": kernel_ms},
@@ -566,8 +685,9 @@ def run_ours(args):
                                   "unit": "TFLOP/s", "frac": f64_achieved / peak64,
                                   "peak_source": "measured in this run: FP64 DFMA-chain probe"},
                      "speedup_f32c_vs_f64": value / f64_value},
-            "accuracy": acc,
+            "accuracy": dict(acc, vs_oracle=acc_oracle),
             "tracking": tracking,
+            "cpu_baseline_tracking": cpu_track,
             "gpu_launches": args.steps,
             "clocks": clocks,
             "cpu_baseline": cpu,
@@ -585,16 +705,19 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--fp64-steps", type=int, default=2)
     ap.add_argument("--points", type=int, default=N_POINTS, help="field points per step (2^20 = the workload)")
-    ap.add_argument("--cpu-points", type=int, default=16384)
+    ap.add_argument("--cpu-points", type=int, default=65536)
     ap.add_argument("--ref-points", type=int, default=4096)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-tracking", action="store_true")
     ap.add_argument("--no-population", action="store_true")
-    ap.add_argument("--track-steps", type=int, default=20, help="timed FP32c RK4 steps of the tracking slice")
+    ap.add_argument("--track-steps", type=int, default=10,
+                    help="timed RK4 steps of the C2 tracking slice (both precisions; C3 takes half)")
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-generation", action="store_true")
     ap.add_argument("--no-speed-test", action="store_true", help="skip the reference's own GPU speed-test slice")
-    ap.add_argument("--adjoint-steps", type=int, default=32, help="RK4 steps of the design-gradient slice")
+    ap.add_argument("--adjoint-steps", type=int, default=256,
+                    help="RK4 steps of the FP32c design-gradient slice (checkpoint every 64)")
+    ap.add_argument("--adjoint-steps-f64", type=int, default=4, help="RK4 steps of the FP64 design-gradient slice")
     ap.add_argument("--traffic", type=float, default=None,
                     help="DRAM bytes per launch of the timed kernel from an ncu capture (default: the committed "
                          "capture of the field-map launch)")

@@ -735,3 +735,52 @@ def field_many(records: Sequence[Dict], pts: numpy.ndarray, processes: int = 1) 
     with ctx.Pool(processes) as pool:
         parts = pool.map(_field_worker, [(list(records), c) for c in chunks if len(c)])
     return numpy.concatenate(parts)
+
+
+# ---------------------------------------------------------------- persistent worker pool (timed CPU baselines)
+_POOL_LINE = None
+
+
+def _pool_init(records):
+    global _POOL_LINE
+    _POOL_LINE = BeamlineOracle(records)
+
+
+def _pool_field(pts):
+    return _POOL_LINE.field_at_points(pts)
+
+
+def _pool_track(args):
+    particle, length, footstep = args
+    return rk4_track(particle, _POOL_LINE.field_at, length, footstep)
+
+
+class OraclePool:
+    """A spawn-started process pool whose workers each build the beamline once, at start-up,
+    and then evaluate fields or track particles on request -- BaseUtils.submit_process_task
+    (base_utils.py:370-444) kept alive between calls, so that a timed CPU baseline measures
+    the field sums and not pool start-up or segment generation."""
+
+    def __init__(self, records: Sequence[Dict], processes: int):
+        import multiprocessing as mp
+        self.processes = max(1, int(processes))
+        self._pool = mp.get_context("spawn").Pool(self.processes, initializer=_pool_init,
+                                                  initargs=(list(records),))
+
+    def field(self, pts: numpy.ndarray) -> numpy.ndarray:
+        chunks = [c for c in numpy.array_split(pts, self.processes * 4) if len(c)]
+        return numpy.concatenate(self._pool.map(_pool_field, chunks))
+
+    def track(self, particles: numpy.ndarray, length: float, footstep: float) -> numpy.ndarray:
+        return numpy.array(self._pool.map(_pool_track, [(numpy.array(p), length, footstep) for p in particles],
+                                          chunksize=1))
+
+    def close(self) -> None:
+        self._pool.close()
+        self._pool.join()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
