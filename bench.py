@@ -372,8 +372,10 @@ def measure_speed_test(rank):
         torch.cuda.synchronize()
         t = time.perf_counter() - t0
     finally:
+        block = engine.particle_block()
         engine.set_units_per_cta(0)
-    out["step_20mm"]["autotuned"] = {"units_per_cta": best, "seconds": t,
+        engine.set_particle_block(0)
+    out["step_20mm"]["autotuned"] = {"units_per_cta": best, "particle_block": block or "automatic", "seconds": t,
                                      "gpairs_per_s": 100 * 16 * n_steps * 4 * warm.segments_of(0) / t / 1e9}
     return out
 

@@ -550,7 +550,7 @@ static int adjoint_grid(int *grid_out) {
 }
 
 static int64_t adjoint_scratch_bound(int n_designs, int64_t n_p, int max_steps, int K) {
-    const int64_t track = track_scratch_bound(n_designs, n_p);
+    const int64_t track = track_scratch_bound(n_designs, n_p, false);   // the adjoint's own particle block
     TrackScratchLayout L{0, 0, 0, 0, track};
     const int n_ckpt = (max_steps + K - 1) / K;
     return adj_layout(L, n_designs, n_p, n_ckpt, K).total;

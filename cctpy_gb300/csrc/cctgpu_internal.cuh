@@ -51,8 +51,10 @@ struct TrackScratchLayout {
 // Scratch layout for n_units units of `group` particles each.
 TrackScratchLayout track_scratch_layout(int n_designs, int64_t n_particles, int64_t n_units, int group);
 // Upper bound of the scratch any precision needs on the current device (or a generous
-// device-independent bound when no device is visible).
-int64_t track_scratch_bound(int n_designs, int64_t n_particles);
+// device-independent bound when no device is visible), with the particle block the forward
+// entry points use (block_setting: the process-wide setting if made) or group_size's (the
+// adjoint's).
+int64_t track_scratch_bound(int n_designs, int64_t n_particles, bool block_setting = true);
 int launch_track_async(const double *kls, const double *p0s, const int64_t *seg_off, const void *packed,
                        const double *qs, const int64_t *qs_off, int n_designs, double *particles, int64_t n_p,
                        double distance, double footstep, int precision, void *scratch, int64_t scratch_bytes,

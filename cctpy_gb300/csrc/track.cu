@@ -244,7 +244,7 @@ int64_t units_bound(int n_designs, int64_t n_p, int G, int grid) {
     return (int64_t)g_units_per_cta * grid + (int64_t)n_designs * ((n_p + G - 1) / G);
 }
 
-int64_t track_scratch_bound(int n_designs, int64_t n_particles) {
+int64_t track_scratch_bound(int n_designs, int64_t n_particles, bool block_setting) {
     int grid = 0;
     if (track_grid(&grid) != CCT_OK) {
         clear_error();
@@ -252,7 +252,7 @@ int64_t track_scratch_bound(int n_designs, int64_t n_particles) {
     }
     int64_t best = 0;
     for (int prec = 0; prec < 2; ++prec) {
-        const int G = track_group(prec, n_particles);
+        const int G = block_setting ? track_group(prec, n_particles) : group_size(prec, n_particles);
         const int64_t t = track_scratch_layout(n_designs, n_particles, units_bound(n_designs, n_particles, G, grid), G).total;
         if (t > best) best = t;
     }

@@ -170,3 +170,16 @@ def test_particle_block_setting(lib):
         lib.cct_track_set_particle_block(0)
     assert lib.cct_track_particle_block() == 0
     assert plan(lib, [46080], 100, 1, 456)[4] == 128
+
+
+def test_adjoint_scratch_ignores_the_particle_block_setting(lib):
+    """cct_track_adjoint plans with the automatic particle block whatever the forward entry
+    points are set to, so its scratch query must not follow the setting (a query made after
+    cct_autotune once returned too little)."""
+    want = lib.cct_adjoint_scratch_bytes(16, 1024, 3, 2)
+    try:
+        for g in (32, 64, 128, 256):
+            lib.cct_track_set_particle_block(g)
+            assert lib.cct_adjoint_scratch_bytes(16, 1024, 3, 2) == want
+    finally:
+        lib.cct_track_set_particle_block(0)
