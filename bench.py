@@ -252,7 +252,7 @@ def measure_tracking(args, dev, rank):
         dsp = engine.design_set_of(bls)
         dsp.packed()
         pp = W.beam_particles(bls[0], 512, seed=2 + rank, kinetic_MeV=215.0)
-        psteps = max(1, steps // 2)
+        psteps = args.population_steps
         res = {}
         for prec in ("f32c", "f64"):
             t = timed(dsp, pp, psteps, prec, reps)
@@ -712,8 +712,10 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-tracking", action="store_true")
     ap.add_argument("--no-population", action="store_true")
-    ap.add_argument("--track-steps", type=int, default=10,
-                    help="timed RK4 steps of the C2 tracking slice (both precisions; C3 takes half)")
+    ap.add_argument("--track-steps", type=int, default=20,
+                    help="timed RK4 steps of the C2 tracking slice (both precisions)")
+    ap.add_argument("--population-steps", type=int, default=5,
+                    help="timed RK4 steps of the C3 population slice (both precisions)")
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-generation", action="store_true")
     ap.add_argument("--no-speed-test", action="store_true", help="skip the reference's own GPU speed-test slice")
