@@ -610,18 +610,22 @@ static int launch_adjoint(const double *kls, const double *p0s, const int64_t *s
     P.state = reinterpret_cast<double *>(sc + L.state_off);
     P.partial = reinterpret_cast<double *>(sc + L.partial_off);
     P.ctrl = reinterpret_cast<unsigned *>(sc);
-    P.unit_off = reinterpret_cast<const int64_t *>(sc + 256);
+    P.unit_off = reinterpret_cast<const int64_t *>(sc + kCtrlBytes);
     P.chunks = P.unit_off + n_designs + 1;
     P.chunk_tiles = P.chunks + n_designs;
     P.precision = precision;
     P.barrier_blocks = (unsigned)(grid + g_test_phantom_blocks);
     P.wait_ns = (unsigned long long)g_wait_ms * 1000000ull;
     P.record = nullptr;
+    P.tiny = 0;                     // the adjoint's forward keeps the chunk partial sums
+    P.tiny_copies = 1;
+    P.tiny_acc = nullptr;
+    P.tiny_bad = nullptr;
     set_flow(P, sc + L.flow_off);   // the forward launches (the reverse sweep keeps its barriers)
 
     // 1. state from the records; learn the step count
-    CCT_TRY_CUDA(cudaMemsetAsync(sc, 0, 256, st));
-    CCT_TRY_CUDA(cudaMemcpyAsync(sc + 256, tables.data(), 8 * tables.size(), cudaMemcpyHostToDevice, st));
+    CCT_TRY_CUDA(cudaMemsetAsync(sc, 0, kCtrlBytes, st));
+    CCT_TRY_CUDA(cudaMemcpyAsync(sc + kCtrlBytes, tables.data(), 8 * tables.size(), cudaMemcpyHostToDevice, st));
     P.init_from_records = 1;
     P.write_back = 0;
     P.step_begin = 0;

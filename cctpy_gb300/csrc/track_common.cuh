@@ -30,6 +30,31 @@ constexpr uint32_t kTmaPolls = 1u << 22;
 // control words (CW_SEQ: a 64-bit counter in words 8-9)
 enum { CW_COUNT = 0, CW_GEN = 1, CW_ERR = 2, CW_NONFINITE = 3, CW_MAXSTEPS = 4, CW_NEXT0 = 5, CW_NEXT1 = 6, CW_SEQ = 8 };
 
+// Control block at the start of the scratch: the words above in its first 128-byte line, then
+// one line per group of units of the small-batch schedule (a 64-bit count of finished units
+// each, on its own line so that the groups' additions do not queue on one L2 line).  The unit
+// tables follow it.
+constexpr int kCtrlBytes = 4096;
+constexpr int kCtrlLineWords = 32;
+constexpr int kTinyGroups = kCtrlBytes / 128 - 1;      // lines 1..31
+constexpr int kCtrlTinyCount = kCtrlLineWords;          // word index of the first group's counter
+
+// Small batches (FP32c, at most kTinyMax particles in fewer than kFlowMinBlocks particle
+// blocks): every CTA owns at most one unit for the whole launch and keeps its own copy of every
+// particle's RK4 state in shared memory.  A unit adds its chunk's field into per-particle
+// fixed-point accumulators (int64, kTinyScale units a tesla; two stage parities; never cleared:
+// a stage's field is the difference from the previous reading of the same parity, exact in
+// integers, so it does not depend on the order the units arrive in) and counts itself done;
+// every CTA waits for the stage's count, reads the accumulators and advances its copy of every
+// particle (all copies identical: same integers, same arithmetic).  No grid barrier and no
+// serial section per stage; a unit whose tiles fit the ring keeps them in shared memory.  The
+// accumulators come in up to kTinyCopies copies (unit u adds into copy u % copies), so that the
+// units' atomic additions spread over more addresses; readers add the copies up.
+constexpr int kTinyMax = 64;
+constexpr int kTinyCopies = 8;    // measured on C0 (32 protons): 2 -> 12.5, 4 -> 10.0, 8 -> 9.1, 12 -> 9.9, 16 -> 10.1 us a stage
+constexpr double kTinyScale = 17592186044416.0;        // 2^44: 5.7e-14 T resolution
+constexpr double kTinyLimit = 262144.0;                 // 2^18 T: far inside the int64 range
+
 // Dataflow schedule (batches of at least kFlowMinBlocks particle blocks): per particle block a
 // 64-bit count of finished chunk units and a 32-bit count of finished stages.
 constexpr int kFlowMinBlocks = 8;
@@ -64,6 +89,12 @@ struct TrackParams {
     int write_back;                // 1: write the final state into the particle records
     int step_begin, step_end;      // steps [step_begin, min(step_end, step count)) run here
     double *record;                // null, or per (step, stage, particle): stage state + field
+    // small-batch schedule (tiny = 1): fixed-point field accumulators and, per particle, a count
+    // of unit fields that were non-finite or out of range
+    int tiny;
+    int tiny_copies;               // copies of the accumulators (1..kTinyCopies)
+    long long *tiny_acc;           // [copies][2][particles][3]
+    unsigned *tiny_bad;            // [copies][2][particles]
     // dataflow schedule (use_flow = 1): per particle block (design d, block b at d * blocks + b)
     int use_flow;
     int flow_skew;                 // test hook: extra stages every wait requires (0 in use)
@@ -84,6 +115,12 @@ struct TrackSmem {
     double red[kRedDoubles];
     int64_t unit;                  // unit handed to this CTA (dynamic schedule)
     int verdict;
+    // small-batch schedule: this CTA's copy of every particle's RK4 state, its last reading of
+    // each stage parity's accumulators (3 components and the flag count) per particle, and each
+    // particle's design's QS record range
+    double tiny_state[kTinyMax * kStateD];
+    long long tiny_prev[2 * kTinyMax * 4];
+    int64_t tiny_qs[kTinyMax][2];
 };
 constexpr uint32_t kNone = 0xffffffffu;
 
@@ -383,10 +420,32 @@ static __device__ __forceinline__ void unit_prefetch(const TrackParams &P, int64
 // claims the CTA's next unit of the phase and issues that unit's first tiles, so that their
 // copies overlap this unit's reduction.  Returns the next unit (>= n_units: none), or -1 if a
 // TMA wait gave up (CCT_ERR_TIMEOUT recorded).
-template <int PPT, bool GRAD, bool FLOW = false>
+// Small-batch schedule: unit u adds its field at particle pi into its copy of the fixed-point
+// accumulators of stage parity `parity` (a component out of range or non-finite counts on the
+// particle's flag instead).
+static __device__ __forceinline__ void tiny_add(const TrackParams &P, int64_t u, int parity, int64_t pi, double x,
+                                                double y, double z) {
+    const int64_t total = (int64_t)P.n_designs * P.n_p;
+    const int64_t slot = ((u % P.tiny_copies) * 2 + parity) * total + pi;
+    unsigned long long *acc = reinterpret_cast<unsigned long long *>(P.tiny_acc + slot * 3);
+    const double v[3] = {x, y, z};
+    bool bad = false;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        if (fabs(v[c]) < kTinyLimit) atomicAdd(acc + c, (unsigned long long)__double2ll_rn(v[c] * kTinyScale));
+        else bad = true;
+    }
+    if (bad) atomicAdd(P.tiny_bad + slot, 1u);
+}
+
+// (TINY: the unit's reduced field goes to the small-batch accumulators; resident: the unit's
+// nt <= kRing tiles already sit in ring slots 0..nt-1 from an earlier stage of this CTA's only
+// unit; known: the unit's description, if the caller has it.)
+template <int PPT, bool GRAD, bool FLOW = false, bool TINY = false>
 static __device__ int64_t unit_sum_f32c(const TrackParams &P, const PointSrc &src, int64_t u, TrackSmem &sm,
-                                        uint32_t &kt, int phase, int64_t n_units, int64_t n_seq = 0) {
-    const UnitRef U = locate_unit(P, u);
+                                        uint32_t &kt, int phase, int64_t n_units, int64_t n_seq = 0,
+                                        bool resident = false, const UnitRef *known = nullptr) {
+    const UnitRef U = known ? *known : locate_unit(P, u);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int G = P.G;
     const int NB = G / (32 * PPT);                 // particle sub-blocks
@@ -411,22 +470,25 @@ static __device__ int64_t unit_sum_f32c(const TrackParams &P, const PointSrc &sr
     F32cAcc<PPT> acc;
     acc.zero();
 
-    const unsigned char *tiles = P.tiles + (P.tile_off[U.d] + U.t_beg) * (int64_t)kTileBytes;
     const int64_t nt = U.t_end - U.t_beg;
     // Warps run through the ring independently: a warp waits only for its next tile to
     // land; the last warp done with a slot refills it with the tile kRing further on.
     bool ok_all = true;
     for (int64_t t = 0; t < nt; ++t) {
         const uint32_t k = kt + (uint32_t)t;
-        const int s = (int)(k % kRing);
-        const bool ok = cctdev::mbar_wait_bounded(&sm.full[s], (k / kRing) & 1u, kTmaPolls);
-        if (!__all_sync(0xffffffffu, ok)) {
-            ok_all = false;
-            break;
+        const int s = resident ? (int)t : (int)(k % kRing);
+        if (!resident) {
+            const bool ok = cctdev::mbar_wait_bounded(&sm.full[s], (k / kRing) & 1u, kTmaPolls);
+            if (!__all_sync(0xffffffffu, ok)) {
+                ok_all = false;
+                break;
+            }
         }
         if (GRAD) tile_grad_f32c<PPT, kGradUnroll>(sm.ring[s], ph, pl, a, acc, g0, g1);
         else tile_f32c<PPT, kTrackUnroll, kTrackRcp>(sm.ring[s], ph, pl, acc, g0, g1);
+        if (resident) continue;
         if (cctdev::ring_release_last(&sm.released[s], kTrackWarps) && t + kRing < nt) {
+            const unsigned char *tiles = P.tiles + (P.tile_off[U.d] + U.t_beg) * (int64_t)kTileBytes;
             sm.last_issued[s] = k + kRing;
             cctdev::fence_proxy_async();
             cctdev::mbar_arrive_expect_tx(&sm.full[s], kTileBytes);
@@ -441,7 +503,7 @@ static __device__ int64_t unit_sum_f32c(const TrackParams &P, const PointSrc &sr
         __syncthreads();
         return -1;
     }
-    kt += (uint32_t)nt;
+    if (!resident) kt += (uint32_t)nt;
     // all warps are past their last tile: claim the next unit and start its copies, so that
     // they overlap this unit's reduction (FLOW: the caller claims after the unit is counted,
     // so that a CTA that then runs a block update holds no claimed unit meanwhile)
@@ -467,6 +529,11 @@ static __device__ int64_t unit_sum_f32c(const TrackParams &P, const PointSrc &sr
             sx += r[0];
             sy += r[1];
             sz += r[2];
+        }
+        if (TINY) {
+            const int64_t j = U.b * G + slot;
+            if (j < P.n_p) tiny_add(P, u, phase & 1, (int64_t)U.d * P.n_p + j, sx, sy, sz);
+            continue;
         }
         double *out = P.partial + (u * G + slot) * 3;
         out[0] = sx;
@@ -597,13 +664,12 @@ __device__ __forceinline__ bool particle_active(const TrackParams &P, int64_t pi
 
 // Phase C for one particle at RK4 stage `stage` (0..3) of step `step`, given the CCT field
 // B (sum of the chunk partials; QS are added here).
-static __device__ void particle_update(const TrackParams &P, int64_t pi, int step, int stage, const double Bc[3]) {
-    double *S = P.state + pi * kStateD;
+static __device__ void particle_update_at(const TrackParams &P, double *S, int64_t pi, int step, int stage,
+                                          const double Bc[3], int64_t q0, int64_t q1) {
     if ((double)step >= S[ST_NSTEPS]) return;
-    const int d = (int)(pi / P.n_p);
     double B[3] = {Bc[0], Bc[1], Bc[2]};
     const double *Ys = S + ST_YS;
-    for (int64_t q = P.qs_off[d]; q < P.qs_off[d + 1]; ++q)
+    for (int64_t q = q0; q < q1; ++q)
         qs_field_add(P.qs + kQsRecord * q, Ys[0], Ys[1], Ys[2], B[0], B[1], B[2]);
     if (P.record) {
         double *rec = P.record + (((int64_t)(step - P.step_begin) * 4 + stage) * ((int64_t)P.n_designs * P.n_p) + pi) * kRec;
@@ -649,6 +715,47 @@ static __device__ void particle_update(const TrackParams &P, int64_t pi, int ste
             finite = finite && isfinite(Y0[c]);
         }
         if (!finite) atomicExch(P.ctrl + CW_NONFINITE, 1u);
+    }
+}
+
+// The same for the particle's state in P.state, with its design's QS records.
+static __device__ __forceinline__ void particle_update(const TrackParams &P, int64_t pi, int step, int stage,
+                                                       const double Bc[3]) {
+    const int d = (int)(pi / P.n_p);
+    particle_update_at(P, P.state + pi * kStateD, pi, step, stage, Bc, P.qs_off[d], P.qs_off[d + 1]);
+}
+
+// Small-batch schedule: after stage `phase` is complete, every particle's field for it from the
+// accumulators of its parity (all copies, read from L2; integer sums, exact in any order) minus
+// this CTA's previous reading of them, and this CTA's copy of the particle advanced.  A thread
+// a particle: the particles' FP64 updates then share as few warps as possible (an FP64 warp
+// instruction costs the FP64 pipe about the same with few lanes active as with all).
+static __device__ void tiny_advance(const TrackParams &P, TrackSmem &sm, int step, int stage, int phase) {
+    const int64_t total = (int64_t)P.n_designs * P.n_p;
+    const int par = phase & 1;
+    for (int64_t pi = threadIdx.x; pi < total; pi += blockDim.x) {
+        unsigned long long a[3] = {0ull, 0ull, 0ull};
+        unsigned bad = 0u;
+        for (int r = 0; r < P.tiny_copies; ++r) {
+            const int64_t slot = ((int64_t)r * 2 + par) * total + pi;
+            const unsigned long long *acc = reinterpret_cast<const unsigned long long *>(P.tiny_acc + slot * 3);
+#pragma unroll
+            for (int c = 0; c < 3; ++c) a[c] += __ldcg(acc + c);
+            bad += __ldcg(P.tiny_bad + slot);
+        }
+        long long *prev = sm.tiny_prev + ((int64_t)par * kTinyMax + pi) * 4;
+        const bool nonfinite = (long long)bad != prev[3];
+        double B[3];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const long long f = (long long)(a[c] - (unsigned long long)prev[c]);
+            B[c] = nonfinite ? __longlong_as_double(0x7ff8000000000000LL) : __ll2double_rn(f) * (1.0 / kTinyScale);
+            prev[c] = (long long)a[c];
+        }
+        prev[3] = (long long)bad;
+        double *S = sm.tiny_state + pi * kStateD;
+        if ((double)step < S[ST_NSTEPS])
+            particle_update_at(P, S, pi, step, stage, B, sm.tiny_qs[pi][0], sm.tiny_qs[pi][1]);
     }
 }
 
@@ -784,5 +891,7 @@ int64_t plan_units(const int64_t *hoff, int n_designs, int64_t n_p, int G, int g
 int64_t units_bound(int n_designs, int64_t n_p, int G, int grid);
 cudaError_t launch_track_kernel(TrackParams &P, int grid, cudaStream_t st);
 void set_flow(TrackParams &P, unsigned char *flow);
+bool tiny_eligible(int precision, int n_designs, int64_t n_p, int G);
+void set_tiny(TrackParams &P, bool eligible, int64_t partial_units);
 
 }  // namespace cctgpu

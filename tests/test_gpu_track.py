@@ -181,11 +181,17 @@ def test_bounded_dataflow_wait_reports_timeout(golden):
     assert np.isfinite(out).all()
 
 
-def test_nonfinite_particle_is_reported(golden):
+@pytest.mark.parametrize("prec", ["f64", "f32c"])
+def test_nonfinite_particle_is_reported(golden, prec):
+    """A NaN velocity (FP32c: a small batch, whose unit fields go through fixed-point
+    accumulators; the NaN position that follows flags the particle there) is reported as
+    CctNonFiniteError, and the other particles are tracked as alone."""
     _, cct = W.build_single_dipole()
     ps = golden["sd_particles_in"][:3].copy()
     ps[1, 3] = np.nan
     with pytest.raises(_lib.CctNonFiniteError):
-        engine.track(engine.design_of(cct), ps, 0.01, 0.001, "f64")
+        engine.track(engine.design_of(cct), ps, 0.01, 0.001, prec)
+    good = engine.track(engine.design_of(cct), ps[[0, 2]], 0.01, 0.001, prec)[0]
+    assert np.isfinite(good).all()
     with pytest.raises(ValueError):
         engine.track(engine.design_of(cct), ps, -1.0, 0.001, "f64")

@@ -183,3 +183,19 @@ def test_adjoint_scratch_ignores_the_particle_block_setting(lib):
             assert lib.cct_adjoint_scratch_bytes(16, 1024, 3, 2) == want
     finally:
         lib.cct_track_set_particle_block(0)
+
+
+def test_small_fp32c_batches_plan_one_unit_per_cta(lib):
+    """FP32c batches of at most 64 particles in fewer than eight particle blocks run the
+    small-batch schedule, in which every CTA keeps one unit for the whole launch: the planner
+    gives them at most one unit a CTA, covering every tile; FP64 and larger batches keep the
+    usual split (here: more units than CTAs)."""
+    grid = 100
+    for seg_counts, n_p in (([597600], 32), ([46080], 32), ([119520, 200000], 16), ([46080] * 4, 16)):
+        units, unit_off, chunks, ct, g = plan(lib, seg_counts, n_p, 1, grid)
+        assert 0 < units <= grid, (seg_counts, n_p, units)
+        for d, n in enumerate(seg_counts):
+            tiles = -(-n // TILE)
+            assert chunks[d] * ct[d] >= tiles and (chunks[d] - 1) * ct[d] < tiles
+    assert plan(lib, [597600], 32, 0, grid)[0] > grid          # FP64: not the small-batch schedule
+    assert plan(lib, [597600], 65, 1, grid)[0] > grid          # more than 64 particles
