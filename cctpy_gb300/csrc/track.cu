@@ -49,7 +49,7 @@ namespace cctgpu {
 // until the unit's particle block has finished the previous stage, after it counts the unit
 // done, and the CTA that finishes a block's stage runs that block's particle update.
 // Returns false if a wait gave up (CCT_ERR_TIMEOUT recorded, ring drained).
-template <int PPT>
+template <int PPT, bool HALF = false>
 static __device__ bool flow_f32c(const TrackParams &P, TrackSmem &sm, uint32_t &kt, int64_t n_units, int64_t n_seq) {
     int64_t s = first_unit();
     if (s < n_seq) unit_prefetch(P, s % n_units, sm, kt);
@@ -63,7 +63,8 @@ static __device__ bool flow_f32c(const TrackParams &P, TrackSmem &sm, uint32_t &
             __syncthreads();
             return false;
         }
-        if (unit_sum_f32c<PPT, false, true>(P, stage_points(P), u, sm, kt, k, n_units, n_seq) < 0) return false;
+        if (unit_sum_f32c<PPT, false, true, false, HALF>(P, stage_points(P), u, sm, kt, k, n_units, n_seq) < 0)
+            return false;
         if (flow_complete(P, sm, blk, k, P.chunks[U.d])) block_update(P, U.d, U.b, k);
         s = claim_seq(P, sm);
         if (s < n_seq) unit_prefetch(P, s % n_units, sm, kt);
@@ -90,7 +91,7 @@ static __device__ bool flow_f64(const TrackParams &P, TrackSmem &sm, int64_t n_u
 // a stage ends when every group's unit counter reaches the stage's count (one warp polls the
 // groups' counters, a lane each).  CTA 0 writes its copy of the final state back.  Returns
 // false if a wait gave up (CCT_ERR_TIMEOUT recorded).
-template <int PPT>
+template <int PPT, bool HALF = false>
 static __device__ bool tiny_track(const TrackParams &P, TrackSmem &sm, uint32_t &kt, int step_end, int64_t n_units) {
     const int64_t total = (int64_t)P.n_designs * P.n_p;
     const int tid = threadIdx.x, lane = tid & 31;
@@ -118,7 +119,7 @@ static __device__ bool tiny_track(const TrackParams &P, TrackSmem &sm, uint32_t 
         for (int stage = 0; stage < 4; ++stage, ++phase) {
             const bool resident = fits && phase > 0;
             if (!resident) unit_prefetch(P, u, sm, kt);
-            if (unit_sum_f32c<PPT, false, true, true>(P, src, u, sm, kt, phase, n_units, 0, resident, &U) < 0)
+            if (unit_sum_f32c<PPT, false, true, true, HALF>(P, src, u, sm, kt, phase, n_units, 0, resident, &U) < 0)
                 return false;
             if (tid < 32) {
                 if (tid == 0) {
@@ -202,12 +203,14 @@ __global__ void __launch_bounds__(kTrackBlock, kTrackMinBlocks) track_kernel(Tra
     if (P.use_flow) {
         const int64_t n_seq = step_end > P.step_begin ? (int64_t)(step_end - P.step_begin) * 4 * n_units : 0;
         if (P.precision == 0) (void)flow_f64(P, sm, n_units, n_seq);
+        else if (P.G == kHalfGroup) (void)flow_f32c<1, true>(P, sm, kt, n_units, n_seq);
         else if (P.ppt == 2) (void)flow_f32c<2>(P, sm, kt, n_units, n_seq);
         else (void)flow_f32c<1>(P, sm, kt, n_units, n_seq);
         if (!grid_barrier(P, sm)) return;   // every stage of every block is done (or a wait gave up)
     }
     if (P.tiny) {
-        if (P.ppt == 2) (void)tiny_track<2>(P, sm, kt, step_end, n_units);
+        if (P.G == kHalfGroup) (void)tiny_track<1, true>(P, sm, kt, step_end, n_units);
+        else if (P.ppt == 2) (void)tiny_track<2>(P, sm, kt, step_end, n_units);
         else (void)tiny_track<1>(P, sm, kt, step_end, n_units);
         if (!grid_barrier(P, sm)) return;   // CTA 0's copy of the state is in P.state (or a wait gave up)
     }
@@ -217,6 +220,8 @@ __global__ void __launch_bounds__(kTrackBlock, kTrackMinBlocks) track_kernel(Tra
             if (P.precision == 0) {
                 for (int64_t u = first_unit(); u < n_units; u = next_unit(P, sm, phase))
                     unit_field_f64(P, u, sm);
+            } else if (P.G == kHalfGroup) {
+                units_f32c<1, false, true>(P, stage_points(P), sm, kt, phase, n_units);
             } else if (P.ppt == 2) {
                 units_f32c<2, false>(P, stage_points(P), sm, kt, phase, n_units);
             } else {
@@ -276,8 +281,11 @@ TrackScratchLayout track_scratch_layout(int n_designs, int64_t n_particles, int6
 // Particles per unit: FP64 keeps 32 (warps split the tiles); FP32c takes the block size that
 // needs the fewest particle slots (blocks x G), the largest of those: e.g. 100 particles run as
 // one block of 128 rather than two of 64 (the same slots), 96 as three blocks of 32.
-int group_size(int precision, int64_t n_p) {
+// min_group 16 (the forward's FP32c tracking) also allows half-warp blocks of 16, for designs
+// of at most 16 particles.
+int group_size(int precision, int64_t n_p, int min_group) {
     if (precision == 0) return 32;
+    if (min_group <= kHalfGroup && n_p <= kHalfGroup) return kHalfGroup;
     int best = kMaxGroup;
     int64_t best_slots = (n_p + best - 1) / best * best;
     for (int G = kMaxGroup / 2; G >= 32; G /= 2) {
@@ -297,7 +305,7 @@ int g_particle_block = 0;   // FP32c particle block set by hand or by cct_autotu
 // assumes.)
 int track_group(int precision, int64_t n_p) {
     if (precision == 1 && g_particle_block != 0) return g_particle_block;
-    return group_size(precision, n_p);
+    return group_size(precision, n_p, kHalfGroup);
 }
 
 int track_grid(int *grid_out) {
@@ -695,8 +703,8 @@ extern "C" int32_t cct_track_units_per_cta(void) { return cctgpu::g_units_per_ct
 
 extern "C" int cct_track_set_particle_block(int32_t particles) {
     cctgpu::clear_error();
-    if (particles != 0 && particles != 32 && particles != 64 && particles != 128 && particles != 256)
-        return cctgpu::set_error(CCT_ERR_ARG, "particle block %d (32, 64, 128 or 256; 0 = automatic)", particles);
+    if (particles != 0 && particles != 16 && particles != 32 && particles != 64 && particles != 128 && particles != 256)
+        return cctgpu::set_error(CCT_ERR_ARG, "particle block %d (16, 32, 64, 128 or 256; 0 = automatic)", particles);
     cctgpu::g_particle_block = particles;
     return CCT_OK;
 }
@@ -705,7 +713,7 @@ extern "C" int32_t cct_track_particle_block(void) { return cctgpu::g_particle_bl
 
 namespace cctgpu {
 static const int kTuneUnits[] = {2, 4, 8, 16, 32};
-static const int kTuneBlocks[] = {32, 64, 128, 256};
+static const int kTuneBlocks[] = {16, 32, 64, 128, 256};
 constexpr int kNumTuneUnits = (int)(sizeof kTuneUnits / sizeof kTuneUnits[0]);
 constexpr int kNumTuneBlocks = (int)(sizeof kTuneBlocks / sizeof kTuneBlocks[0]);
 static int64_t up256(int64_t b) { return (b + 255) / 256 * 256; }

@@ -16,6 +16,7 @@ constexpr int kTrackMinBlocks = 3;
 constexpr int kTrackWarps = kTrackBlock / 32;
 static_assert((kTile / kTrackWarps) % kSub == 0, "tile slices hold whole FP32c sub-blocks");
 constexpr int kMaxGroup = 64 * kTrackWarps;   // particles per unit: 2 per lane in every warp
+constexpr int kHalfGroup = 16;                 // smallest FP32c particle block: a particle per half-warp lane
 constexpr int kStateD = 24;          // doubles of RK4 state per particle
 constexpr int kMaxChunks = 4096;     // chunks per (design, block)
 constexpr int kUnitsPerCta = 8;      // default target units per CTA and stage (dynamic load balance)
@@ -441,22 +442,27 @@ static __device__ __forceinline__ void tiny_add(const TrackParams &P, int64_t u,
 // (TINY: the unit's reduced field goes to the small-batch accumulators; resident: the unit's
 // nt <= kRing tiles already sit in ring slots 0..nt-1 from an earlier stage of this CTA's only
 // unit; known: the unit's description, if the caller has it.)
-template <int PPT, bool GRAD, bool FLOW = false, bool TINY = false>
+// HALF: blocks of kHalfGroup particles (PPT 1): lanes l and l + 16 of a warp hold particle l,
+// the two half-warps take different 16-segment halves of a sub-block (8 slices of each tile).
+template <int PPT, bool GRAD, bool FLOW = false, bool TINY = false, bool HALF = false>
 static __device__ int64_t unit_sum_f32c(const TrackParams &P, const PointSrc &src, int64_t u, TrackSmem &sm,
                                         uint32_t &kt, int phase, int64_t n_units, int64_t n_seq = 0,
                                         bool resident = false, const UnitRef *known = nullptr) {
+    static_assert(!HALF || (PPT == 1 && !GRAD), "half-warp blocks: one particle a lane, forward sums only");
     const UnitRef U = known ? *known : locate_unit(P, u);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int G = P.G;
-    const int NB = G / (32 * PPT);                 // particle sub-blocks
-    const int S = kTrackWarps / NB;                // slices of each tile
-    const int sb = warp % NB, sl = warp / NB;
+    const int NB = HALF ? 1 : G / (32 * PPT);                      // particle sub-blocks
+    const int S = HALF ? 2 * kTrackWarps : kTrackWarps / NB;       // slices of each tile
+    const int sb = HALF ? 0 : warp % NB;
+    const int sl = HALF ? 2 * warp + (lane >> 4) : warp / NB;
+    const int pl0 = HALF ? (lane & 15) : sb * 32 * PPT + lane;       // this lane's first particle slot
     const int g0 = sl * (kTile / 4 / S), g1 = g0 + kTile / 4 / S;
 
     float ph[PPT][3], pl[PPT][3], a[PPT][3];
 #pragma unroll
     for (int i = 0; i < PPT; ++i) {
-        int64_t j = U.b * G + sb * 32 * PPT + i * 32 + lane;
+        int64_t j = U.b * G + pl0 + i * 32;
         if (j >= P.n_p) j = P.n_p - 1;
         const int64_t pi = (int64_t)U.d * P.n_p + j;
         const double *Ys = src.pos + pi * src.pos_stride;
@@ -485,7 +491,7 @@ static __device__ int64_t unit_sum_f32c(const TrackParams &P, const PointSrc &sr
             }
         }
         if (GRAD) tile_grad_f32c<PPT, kGradUnroll>(sm.ring[s], ph, pl, a, acc, g0, g1);
-        else tile_f32c<PPT, kTrackUnroll, kTrackRcp>(sm.ring[s], ph, pl, acc, g0, g1);
+        else tile_f32c<PPT, kTrackUnroll, kTrackRcp, HALF ? kSub / 8 : kSub / 4>(sm.ring[s], ph, pl, acc, g0, g1);
         if (resident) continue;
         if (cctdev::ring_release_last(&sm.released[s], kTrackWarps) && t + kRing < nt) {
             const unsigned char *tiles = P.tiles + (P.tile_off[U.d] + U.t_beg) * (int64_t)kTileBytes;
@@ -516,7 +522,7 @@ static __device__ int64_t unit_sum_f32c(const TrackParams &P, const PointSrc &sr
     // reduce the S slices of every particle in fixed order
 #pragma unroll
     for (int i = 0; i < PPT; ++i) {
-        double *r = sm.red + ((size_t)sl * G + sb * 32 * PPT + i * 32 + lane) * 3;
+        double *r = sm.red + ((size_t)sl * G + pl0 + i * 32) * 3;
         r[0] = acc.total(i, 0);
         r[1] = acc.total(i, 1);
         r[2] = acc.total(i, 2);
@@ -545,13 +551,13 @@ static __device__ int64_t unit_sum_f32c(const TrackParams &P, const PointSrc &sr
 }
 
 // All FP32c units of one phase handed to this CTA.  Returns false if a TMA wait gave up.
-template <int PPT, bool GRAD>
+template <int PPT, bool GRAD, bool HALF = false>
 static __device__ bool units_f32c(const TrackParams &P, const PointSrc &src, TrackSmem &sm, uint32_t &kt, int phase,
                                   int64_t n_units) {
     int64_t u = first_unit();
     if (u < n_units) unit_prefetch(P, u, sm, kt);
     while (u < n_units) {
-        u = unit_sum_f32c<PPT, GRAD>(P, src, u, sm, kt, phase, n_units);
+        u = unit_sum_f32c<PPT, GRAD, false, false, HALF>(P, src, u, sm, kt, phase, n_units);
         if (u < 0) return false;
     }
     return true;
@@ -883,7 +889,7 @@ extern int g_test_phantom_blocks;
 extern int g_test_flow_skew;
 extern long long g_wait_ms;
 extern int g_particle_block;
-int group_size(int precision, int64_t n_p);
+int group_size(int precision, int64_t n_p, int min_group = 32);
 int track_group(int precision, int64_t n_p);
 int track_grid(int *grid_out);
 int64_t plan_units(const int64_t *hoff, int n_designs, int64_t n_p, int G, int grid, int64_t max_units, int64_t *unit_off,

@@ -195,3 +195,24 @@ def test_nonfinite_particle_is_reported(golden, prec):
     assert np.isfinite(good).all()
     with pytest.raises(ValueError):
         engine.track(engine.design_of(cct), ps, -1.0, 0.001, "f64")
+
+
+@pytest.mark.parametrize("n_designs", [1, 5, 9])
+def test_half_warp_blocks_of_16_protons(golden, n_designs):
+    """FP32c designs of 16 protons run in blocks of 16 (lanes l and l + 16 of a warp hold
+    proton l and sum different halves of each sub-block): one design on the small-batch
+    schedule, five on grid barriers, nine on the dataflow schedule.  Every copy tracks the
+    reference's 16 protons to 1 um, the same as alone to FP32 rounding, and the same as the
+    FP64 kernel to 1 um."""
+    _, cct = W.build_single_dipole()
+    parts = golden["sd_particles_in"][:16]
+    L = W.single_dipole_track_length()
+    ds = engine.design_set_of([cct] * n_designs)
+    out = engine.track(ds, np.stack([parts] * n_designs), L, 0.001, "f32c")
+    one = engine.track(engine.design_of(cct), parts, L, 0.001, "f32c")[0]
+    f64 = engine.track(engine.design_of(cct), parts, L, 0.001, "f64")[0]
+    for d in range(n_designs):
+        check(out[d], golden["sd_particles_out"][:16], POS_TOL_F32C, 1e-6)
+        np.testing.assert_array_equal(out[d], out[0])
+        assert np.abs(out[d][:, 0:3] - one[:, 0:3]).max() < 1e-8
+        assert np.abs(out[d][:, 0:3] - f64[:, 0:3]).max() < POS_TOL_F32C

@@ -42,6 +42,8 @@ def plan(lib, seg_counts, n_p, precision, grid, max_units=0):
 def expected_group(precision, n_p):
     if precision == 0:
         return 32
+    if n_p <= 16:              # FP32c: half-warp blocks for designs of at most 16 particles
+        return 16
     best, slots = 256, -(-n_p // 256) * 256
     for G in (128, 64, 32):
         s = -(-n_p // G) * G
@@ -151,19 +153,19 @@ def test_particle_block_setting(lib):
     try:
         assert lib.cct_track_particle_block() == 0
         assert plan(lib, [46080], 4096, 1, 456)[4] == 256
-        for g in (32, 64, 128, 256):
+        for g in (16, 32, 64, 128, 256):
             assert lib.cct_track_set_particle_block(g) == _lib.CCT_OK
             assert lib.cct_track_particle_block() == g
             units, unit_off, chunks, ct, got = plan(lib, [46080, 12345], 4096, 1, 456)
             assert got == g
             assert units == unit_off[-1] and np.all(unit_off[1:] - unit_off[:-1] == (4096 // g) * chunks)
             assert plan(lib, [46080], 4096, 0, 456)[4] == 32
-        for bad in (-1, 16, 48, 512):
+        for bad in (-1, 8, 48, 512):
             assert lib.cct_track_set_particle_block(bad) == _lib.CCT_ERR_ARG
         assert lib.cct_track_particle_block() == 256          # a refused value leaves the setting alone
         # every split the autotuner tries fits the scratch it asks for
         need = lib.cct_autotune_scratch_bytes(1, 4096)
-        for g in (32, 64, 128, 256):
+        for g in (16, 32, 64, 128, 256):
             lib.cct_track_set_particle_block(g)
             assert need >= lib.cct_track_scratch_bytes(1, 4096) + 80 * 4096
     finally:
@@ -199,3 +201,15 @@ def test_small_fp32c_batches_plan_one_unit_per_cta(lib):
             assert chunks[d] * ct[d] >= tiles and (chunks[d] - 1) * ct[d] < tiles
     assert plan(lib, [597600], 32, 0, grid)[0] > grid          # FP64: not the small-batch schedule
     assert plan(lib, [597600], 65, 1, grid)[0] > grid          # more than 64 particles
+
+
+def test_half_warp_blocks_for_designs_of_up_to_16_particles(lib):
+    """FP32c designs of at most 16 particles get blocks of 16 (a particle per half-warp lane,
+    so that no lane idles); 17 particles and FP64 keep blocks of 32; the adjoint's scratch
+    query stays on blocks of 32 or more."""
+    for n_p in (1, 5, 16):
+        assert plan(lib, [24000] * 100, n_p, 1, 456)[4] == 16
+        assert plan(lib, [24000] * 100, n_p, 0, 456)[4] == 32
+    assert plan(lib, [24000] * 100, 17, 1, 456)[4] == 32
+    units, unit_off, chunks, ct, g = plan(lib, [24000] * 100, 16, 1, 456)
+    assert units == unit_off[-1] and np.all(unit_off[1:] - unit_off[:-1] == chunks)
