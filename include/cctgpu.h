@@ -165,9 +165,10 @@ int cct_track_status(const void *d_scratch, void *stream);
  *  - units of (design, particle block, segment chunk) per CTA and RK4 stage
  *    (default 8; 1..64, 0 restores the default);
  *  - the FP32c particle block: particles whose field sums a unit computes
- *    together (32, 64, 128 or 256; 0 = automatic, the power of two that needs
- *    the fewest particle slots, the largest of those).  FP64 tracking always
- *    uses blocks of 32, and cct_track_adjoint the automatic choice.
+ *    together (16, 32, 64, 128 or 256; 0 = automatic: 16 for designs of at most
+ *    16 particles, else the power of two from 32 that needs the fewest particle
+ *    slots, the largest of those).  FP64 tracking always uses blocks of 32, and
+ *    cct_track_adjoint the automatic choice from 32 up.
  * cct_autotune times a few RK4 steps of the caller's problem (`steps` steps of
  * `footstep`, on a copy of d_particles, which is not modified) for every
  * particle block from the automatic one up to the first that holds all of a
