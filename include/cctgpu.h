@@ -122,8 +122,12 @@ int cct_field_host(const double *h_kls, const double *h_p0s, int64_t n_seg,
  * One cooperative persistent launch; CTAs take (design, particle block,
  * segment chunk) units from a work counter.  With 8 or more particle blocks
  * each block advances stage by stage as soon as its own units are done
- * (bounded waits on per-block counters); smaller batches meet at bounded
- * grid barriers between RK4 stages.  Needs caller-provided device scratch of
+ * (bounded waits on per-block counters); FP32c batches of at most 64
+ * particles in fewer blocks keep one unit per CTA and a copy of every
+ * particle's state in each CTA, summing fields in fixed-point integers and
+ * waiting (bounded) on per-group unit counters between stages; other smaller
+ * batches meet at bounded grid barriers between RK4 stages.  Results do not
+ * depend on which CTA ran which unit.  Needs caller-provided device scratch of
  * cct_track_scratch_bytes() bytes (256-byte aligned); a smaller buffer is
  * accepted down to the particle state plus one chunk per (design, particle
  * block), the work then being cut into fewer, larger units.  Returns
