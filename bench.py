@@ -702,7 +702,12 @@ def run_ours(args):
     e2e = world * PAIRS * args.steps / e2e_s / 1e9
 
     tracking = None if args.no_tracking else measure_tracking(args, dev, rank)
-    shard = None if args.no_tracking or args.no_population else measure_population_shard(args, rank, world, dist)
+    shard = None
+    if not (args.no_tracking or args.no_population):
+        try:
+            shard = measure_population_shard(args, rank, world, dist)
+        except Exception as e:   # the headline line is printed whatever happens to this leg
+            shard = {"error": f"{type(e).__name__}: {e}"[:300]}
 
     line = None
     if rank == 0:
