@@ -252,12 +252,12 @@ def measure_tracking(args, dev, rank):
         dsp = engine.design_set_of(bls)
         dsp.packed()
         pp = W.beam_particles(bls[0], 512, seed=2 + rank, kinetic_MeV=215.0)
-        psteps = args.population_steps
+        psteps, preps = args.population_steps, 1     # one repetition each: FP64 takes ~20 s a call
         res = {}
         for prec in ("f32c", "f64"):
-            t = timed(dsp, pp, psteps, prec, reps)
+            t = timed(dsp, pp, psteps, prec, preps)
             r = 64 * 512 * psteps / t
-            res[prec] = {"steps": psteps, "reps": reps, "seconds": t, "particle_steps_per_s": r,
+            res[prec] = {"steps": psteps, "reps": preps, "seconds": t, "particle_steps_per_s": r,
                          "gpairs_per_s": 512 * psteps * 4 * dsp.n_segments / t / 1e9}
         segs = [dsp.segments_of(d) for d in range(64)]
         out["design_population"] = dict(
@@ -265,7 +265,7 @@ def measure_tracking(args, dev, rank):
                      "one launch",
             speedup_f32c_vs_f64=res["f32c"]["particle_steps_per_s"] / res["f64"]["particle_steps_per_s"], **res)
         out["design_population"]["f32c_graph_replay"] = measure_graph_replay(dsp, pp, psteps)
-        out["design_population"]["f32c_autotuned"] = tuned(dsp, pp, psteps, 512, reps)
+        out["design_population"]["f32c_autotuned"] = tuned(dsp, pp, psteps, 512, preps)
     if not args.no_speed_test:
         out["reference_speed_test"] = measure_speed_test(rank)
     if not args.no_adjoint:
@@ -774,7 +774,7 @@ def main():
     ap.add_argument("--no-population", action="store_true")
     ap.add_argument("--track-steps", type=int, default=20,
                     help="timed RK4 steps of the C2 tracking slice (both precisions)")
-    ap.add_argument("--population-steps", type=int, default=5,
+    ap.add_argument("--population-steps", type=int, default=10,
                     help="timed RK4 steps of the C3 population slice (both precisions)")
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-generation", action="store_true")
