@@ -127,7 +127,9 @@ static __device__ bool tiny_track(const TrackParams &P, TrackSmem &sm, uint32_t 
                     atomicAdd(mine, 1ull);
                 }
                 __syncwarp();
-                const unsigned long long want = (unsigned long long)(phase + 1) * (unsigned long long)lane_units;
+                // (test hook: flow_skew more stages than exist, so that the wait runs out)
+                const unsigned long long want =
+                    (unsigned long long)(phase + 1 + P.flow_skew) * (unsigned long long)lane_units;
                 const volatile unsigned long long *c = counts + lane * (kCtrlLineWords / 2);
                 volatile int *err = reinterpret_cast<volatile int *>(P.ctrl + CW_ERR);
                 int ok = 1;

@@ -338,11 +338,12 @@ int cct_probe_fma_peak(int kind, double *flops_per_s);
  * context stays usable.  Process-wide; not for production use. */
 int cct_test_set_barrier_fault(int phantom_blocks, int wait_ms);
 
-/* Test hook for the dataflow schedule (batches of 8 or more particle blocks):
- * every wait of a unit for its particle block then requires `stages_ahead`
- * more finished stages than the unit needs, so with stages_ahead >= 1 the
- * first waits never end; the wait limit becomes `wait_ms` (<= 0 restores the
- * 60 s default).  A tracking call then returns CCT_ERR_TIMEOUT after about
+/* Test hook for the dataflow schedule (batches of 8 or more particle blocks)
+ * and the small-batch schedule (FP32c, at most 64 particles): every wait of a
+ * unit for its particle block, or of a CTA for a stage's unit count, then
+ * requires `stages_ahead` more finished stages than it needs, so with
+ * stages_ahead >= 1 the first waits never end; the wait limit becomes
+ * `wait_ms` (<= 0 restores the 60 s default).  A tracking call then returns CCT_ERR_TIMEOUT after about
  * wait_ms and the context stays usable.  No counterpart in the reference.
  * Process-wide; not for production use. */
 int cct_test_set_flow_fault(int stages_ahead, int wait_ms);

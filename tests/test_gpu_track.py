@@ -216,3 +216,21 @@ def test_half_warp_blocks_of_16_protons(golden, n_designs):
         np.testing.assert_array_equal(out[d], out[0])
         assert np.abs(out[d][:, 0:3] - one[:, 0:3]).max() < 1e-8
         assert np.abs(out[d][:, 0:3] - f64[:, 0:3]).max() < POS_TOL_F32C
+
+
+def test_bounded_small_batch_wait_reports_timeout(golden):
+    """A small FP32c batch (the small-batch schedule: CTAs wait on unit counters between
+    stages); the test hook makes every such wait ask for a stage more than exists: it gives
+    up after the wait limit, reports CCT_ERR_TIMEOUT, and the context stays usable."""
+    _, cct = W.build_single_dipole()
+    ds = engine.design_of(cct)
+    parts = golden["sd_particles_in"][:8]
+    lib = _lib.load()
+    lib.cct_test_set_flow_fault(1, 300)
+    try:
+        with pytest.raises(_lib.CctTimeoutError):
+            engine.track(ds, parts, 0.01, 0.001, "f32c")
+    finally:
+        lib.cct_test_set_flow_fault(0, 0)
+    out = engine.track(ds, parts, 0.01, 0.001, "f32c")
+    assert np.isfinite(out).all()
