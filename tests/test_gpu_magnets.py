@@ -10,7 +10,7 @@ pytestmark = pytest.mark.gpu
 
 torch = pytest.importorskip("torch")
 
-from cctpy_gb300 import GPU_ACCELERATOR, MM, P2, P3, Beamline, LocalCoordinateSystem, engine
+from cctpy_gb300 import GPU_ACCELERATOR, MM, P2, P3, Beamline, LocalCoordinateSystem, engine, workloads as W
 from cctpy_gb300.geometry import FunctionLine3
 from cctpy_gb300.magnets import AGCCT_CONNECTOR, CCT, CombinedMagnet, UniformMagnet, Wire
 from cctpy_gb300.particles import RunningParticle
@@ -110,3 +110,17 @@ def test_device_design_set_with_wire(gm):
     bh = engine.field_at_points(host, gm["con_pts"], "f64")
     bd = engine.field_at_points(dev, gm["con_pts"], "f64")
     assert close(bd, bh, 1e-11)
+
+
+def test_small_batch_with_a_design_without_segments(gm, golden):
+    """One small FP32c launch (the small-batch schedule) over a design with no current
+    elements (a quadrupole and a straight dipole) and the single CCT dipole: the first design
+    tracks as cctpy does (analytic fields only), the second as it does alone."""
+    bq = bq_beamline()
+    _, cct = W.build_single_dipole()
+    L = float(gm["bq_length"][0])
+    parts = np.stack([gm["bq_particles_in"], golden["sd_particles_in"][:2]])
+    out = engine.track(engine.design_set_of([bq, cct]), parts, L, 5 * MM, "f32c")
+    assert np.abs(out[0][:, 0:3] - gm["bq_particles_out"][:, 0:3]).max() <= 1e-12
+    alone = engine.track(engine.design_of(cct), golden["sd_particles_in"][:2], L, 5 * MM, "f32c")[0]
+    assert np.abs(out[1][:, 0:3] - alone[:, 0:3]).max() <= 1e-8
