@@ -13,7 +13,9 @@ Measured on GB300 (max over the fixture points): fields within 6.1e-14 T of cctp
 (single dipole, points to 8 mm from the windings), 1.8e-14 T (second section), 3.5e-14 T
 (gantry section), 4.8e-15 T (first section), 1.2e-15 T (QS beamline): at most 1.7e-14 of |B|
 plus 5e-15 T, the rounding of the global FP64 segment coordinates the reference's GPU format
-carries.
+carries.  FP64 tracks: within 8.9e-15 m of cctpy's final positions (the whole single-dipole arc
+at 1 mm, both sections at 100 mm, the gantry section at 50 mm, two population designs) and
+relative velocities within 2.4e-15.
 """
 import json
 import os
@@ -31,8 +33,8 @@ from tests.conftest import GOLDEN, reference_design
 FIELD_RTOL = 3e-14    # of |B|, FP64 GPU vs cctpy's CPU sum at every fixture point
 FIELD_ATOL = 5e-15    # tesla
 KNOWN_ATOL = 1e-14    # tesla: the reference's own assertion (ccpty_cuda.py:1176)
-TRACK_POS_TOL = 1e-12  # metres after the whole track, FP64 GPU vs cctpy's CPU track
-TRACK_VEL_RTOL = 1e-12
+TRACK_POS_TOL = 1e-13  # metres after the whole track, FP64 GPU vs cctpy's CPU track (its ~1e-10 mm)
+TRACK_VEL_RTOL = 1e-13
 
 
 def _records(name):

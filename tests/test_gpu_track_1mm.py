@@ -4,7 +4,8 @@ designs of the seeded population with 4 protons each, over a 1.0 m window from s
 the design orbit (the end of the entrance drift and the first dipole's entrance), 1000 RK4
 steps.  The package builds the beamlines as a user would; both precisions are held to the
 tolerances of the other tracking tests, and the FP64 tracks on cctpy's own segment placement
-(`reference_design`) to the drop-in's 1e-12 m."""
+(`reference_design`) to 1e-13 m, the agreement the reference states for its own FP64 GPU
+tracks."""
 import json
 import os
 
@@ -19,7 +20,7 @@ from cctpy_gb300 import HUST_SC_GANTRY, engine, workloads as W
 from tests.conftest import GOLDEN, reference_design
 
 TOL = {"f64": (1e-9, 1e-9), "f32c": (1e-6, 1e-6)}   # position (m), velocity (relative to |v|)
-REF_POS_TOL = 1e-12
+REF_POS_TOL = 1e-13     # measured: 8.9e-16, 6.2e-16, 5.8e-14 m
 
 
 @pytest.fixture(scope="module")
