@@ -542,6 +542,25 @@ def measure_design_grads(args, rank):
     return out
 
 
+def add_pipe_fractions(node, peak32: float, peak64: float, prec: str = None):
+    """Beside every Gpairs/s figure of the tracking block, its fraction of this run's measured
+    FMA-pipe peak at 26 flop a pair: FP32 for FP32c lines, FP64 for FP64 lines (the adjoint's
+    forward-equivalent rate included)."""
+    if isinstance(node, dict):
+        for k, v in list(node.items()):
+            p = prec
+            if k.startswith("f32c") or k in ("reference_speed_test", "optimiser_generation"):   # FP32c only
+                p = "f32c"
+            elif k.startswith("f64"):
+                p = "f64"
+            if isinstance(v, dict):
+                add_pipe_fractions(v, peak32, peak64, p)
+            elif isinstance(v, (int, float)) and p and k.endswith("gpairs_per_s"):
+                peak = peak32 if p == "f32c" else peak64
+                node[k.replace("gpairs_per_s", "frac_of_") + ("fp32_pipe" if p == "f32c" else "fp64_pipe")] = \
+                    FLOPS_PER_PAIR * v * 1e9 / peak
+
+
 # ---------------------------------------------------------------- CPU baselines beside the GPU arm
 def measure_cpu_baselines(args, ds):
     """The oracle on the machine's host cores (rank 0, one GPU): field sums on args.cpu_points of the
@@ -702,6 +721,8 @@ def run_ours(args):
     e2e = world * PAIRS * args.steps / e2e_s / 1e9
 
     tracking = None if args.no_tracking else measure_tracking(args, dev, rank)
+    if tracking is not None:
+        add_pipe_fractions(tracking, peak32 * 1e12, peak64 * 1e12)
     shard = None
     if not (args.no_tracking or args.no_population):
         try:
