@@ -103,6 +103,11 @@ static __device__ bool tiny_track(const TrackParams &P, TrackSmem &sm, uint32_t 
         sm.tiny_qs[pi][1] = P.qs_off[d + 1];
     }
     __syncthreads();
+    for (int64_t pi = tid; pi < total; pi += blockDim.x)   // positions as double-float pairs
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+            split_df(sm.tiny_state[pi * kStateD + ST_YS + c], sm.tiny_pts[pi][c], sm.tiny_pts[pi][3 + c]);
+    __syncthreads();
     const int64_t u = blockIdx.x;
     if (u >= n_units) return true;   // no unit: nothing to do until the final barrier (CTA 0 has unit 0)
     const UnitRef U = locate_unit(P, u);
@@ -162,15 +167,15 @@ static __device__ bool tiny_track(const TrackParams &P, TrackSmem &sm, uint32_t 
     return true;
 }
 
-__global__ void __launch_bounds__(kTrackBlock, kTrackMinBlocks) track_kernel(TrackParams P) {
-    __shared__ __align__(128) TrackSmem sm;
+// Start of every tracking launch: state from the particle records with the step count and dt
+// as the CPU reference computes them (init_from_records), the small-batch accumulators
+// cleared, the unit counters reset; ends at the first grid barrier.  Returns false if the
+// device-side plan rejected the inputs or the barrier gave up; else the launch's last step.
+static __device__ bool track_begin(const TrackParams &P, TrackSmem &sm, int &step_end) {
     const int64_t total = (int64_t)P.n_designs * P.n_p;
     const int64_t tstride = (int64_t)gridDim.x * blockDim.x;
-    if (*(volatile unsigned *)(P.ctrl + CW_ERR) != 0) return;   // the device-side plan rejected the inputs
+    if (*(volatile unsigned *)(P.ctrl + CW_ERR) != 0) return false;   // the device-side plan rejected the inputs
     if (threadIdx.x == 0) ring_init(sm);
-    uint32_t kt = 0;   // tiles consumed through the ring by this CTA
-
-    // init: state from the particle records; step count and dt as the CPU reference computes them
     for (int64_t pi = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; P.init_from_records && pi < total;
          pi += tstride) {
         const double *r = P.particles + pi * 10;
@@ -195,9 +200,31 @@ __global__ void __launch_bounds__(kTrackBlock, kTrackMinBlocks) track_kernel(Tra
         }
     }
     clear_unit_counters(P);
-    if (!grid_barrier(P, sm)) return;
+    if (!grid_barrier(P, sm)) return false;
     const int max_steps = P.init_from_records ? (int)*(volatile unsigned *)(P.ctrl + CW_MAXSTEPS) : P.step_end;
-    const int step_end = min(max_steps, P.step_end);
+    step_end = min(max_steps, P.step_end);
+    return true;
+}
+
+// End of a tracking launch: the final state into the particle records (write_back).
+static __device__ void track_end(const TrackParams &P) {
+    const int64_t total = (int64_t)P.n_designs * P.n_p;
+    const int64_t tstride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t pi = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; P.write_back && pi < total; pi += tstride) {
+        double *r = P.particles + pi * 10;
+        const double *S = P.state + pi * kStateD;
+        for (int c = 0; c < 6; ++c) r[c] = S[ST_Y0 + c];
+        if (S[ST_NSTEPS] > 0.0) r[9] = r[9] + P.distance;
+    }
+}
+
+// The dataflow and grid-barrier schedules.
+__global__ void __launch_bounds__(kTrackBlock, kTrackMinBlocks) track_kernel(TrackParams P) {
+    __shared__ __align__(128) TrackSmem sm;
+    const int64_t total = (int64_t)P.n_designs * P.n_p;
+    int step_end = 0;
+    if (!track_begin(P, sm, step_end)) return;
+    uint32_t kt = 0;   // tiles consumed through the ring by this CTA
     const int64_t n_units = P.unit_off[P.n_designs];
     const int64_t gwarp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
@@ -210,14 +237,8 @@ __global__ void __launch_bounds__(kTrackBlock, kTrackMinBlocks) track_kernel(Tra
         else (void)flow_f32c<1>(P, sm, kt, n_units, n_seq);
         if (!grid_barrier(P, sm)) return;   // every stage of every block is done (or a wait gave up)
     }
-    if (P.tiny) {
-        if (P.G == kHalfGroup) (void)tiny_track<1, true>(P, sm, kt, step_end, n_units);
-        else if (P.ppt == 2) (void)tiny_track<2>(P, sm, kt, step_end, n_units);
-        else (void)tiny_track<1>(P, sm, kt, step_end, n_units);
-        if (!grid_barrier(P, sm)) return;   // CTA 0's copy of the state is in P.state (or a wait gave up)
-    }
     int phase = 0;
-    for (int step = P.step_begin; !P.use_flow && !P.tiny && step < step_end; ++step) {
+    for (int step = P.step_begin; !P.use_flow && step < step_end; ++step) {
         for (int stage = 0; stage < 4; ++stage, ++phase) {
             if (P.precision == 0) {
                 for (int64_t u = first_unit(); u < n_units; u = next_unit(P, sm, phase))
@@ -250,18 +271,29 @@ __global__ void __launch_bounds__(kTrackBlock, kTrackMinBlocks) track_kernel(Tra
         }
     }
 
-    for (int64_t pi = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; P.write_back && pi < total; pi += tstride) {
-        double *r = P.particles + pi * 10;
-        const double *S = P.state + pi * kStateD;
-        for (int c = 0; c < 6; ++c) r[c] = S[ST_Y0 + c];
-        if (S[ST_NSTEPS] > 0.0) r[9] = r[9] + P.distance;
-    }
+    track_end(P);
+}
+
+// The small-batch schedule, a kernel of its own so that its code does not weigh on the other
+// schedules' register allocation.
+__global__ void __launch_bounds__(kTrackBlock, kTrackMinBlocks) track_tiny_kernel(TrackParams P) {
+    __shared__ __align__(128) TrackSmem sm;
+    int step_end = 0;
+    if (!track_begin(P, sm, step_end)) return;
+    uint32_t kt = 0;
+    const int64_t n_units = P.unit_off[P.n_designs];
+    if (P.G == kHalfGroup) (void)tiny_track<1, true>(P, sm, kt, step_end, n_units);
+    else if (P.ppt == 2) (void)tiny_track<2>(P, sm, kt, step_end, n_units);
+    else (void)tiny_track<1>(P, sm, kt, step_end, n_units);
+    if (!grid_barrier(P, sm)) return;   // CTA 0's copy of the state is in P.state (or a wait gave up)
+    track_end(P);
 }
 
 // ---------------------------------------------------------------- host side
 cudaError_t launch_track_kernel(TrackParams &P, int grid, cudaStream_t st) {
     void *args[] = {&P};
-    return cudaLaunchCooperativeKernel((const void *)track_kernel, dim3(grid), dim3(kTrackBlock), args, 0, st);
+    const void *fn = P.tiny ? (const void *)track_tiny_kernel : (const void *)track_kernel;
+    return cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(kTrackBlock), args, 0, st);
 }
 
 int g_test_phantom_blocks = 0;
@@ -316,7 +348,11 @@ int track_grid(int *grid_out) {
     CCT_TRY_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     CCT_TRY_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
     if (!coop) return set_error(CCT_ERR_UNSUPPORTED, "device %d has no cooperative launch", dev);
+    // both tracking kernels are launched with this grid: the smaller of their occupancies
+    int per_sm_tiny = 0;
     CCT_TRY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, track_kernel, kTrackBlock, 0));
+    CCT_TRY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_tiny, track_tiny_kernel, kTrackBlock, 0));
+    per_sm = std::min(per_sm, per_sm_tiny);
     if (per_sm < 1) return set_error(CCT_ERR_UNSUPPORTED, "tracking kernel does not fit on an SM");
     *grid_out = sms * per_sm;
     return CCT_OK;
@@ -606,7 +642,7 @@ int launch_track_async(const double *kls, const double *p0s, const int64_t *seg_
     attr[0].val.cooperative = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    CCT_TRY_CUDA(cudaLaunchKernelEx(&cfg, track_kernel, P));
+    CCT_TRY_CUDA(cudaLaunchKernelEx(&cfg, P.tiny ? track_tiny_kernel : track_kernel, P));
     return CCT_OK;
 }
 

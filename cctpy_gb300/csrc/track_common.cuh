@@ -122,6 +122,7 @@ struct TrackSmem {
     double tiny_state[kTinyMax * kStateD];
     long long tiny_prev[2 * kTinyMax * 4];
     int64_t tiny_qs[kTinyMax][2];
+    float tiny_pts[kTinyMax][6];   // each particle's stage position as double-float (hi xyz, lo xyz)
 };
 constexpr uint32_t kNone = 0xffffffffu;
 
@@ -421,19 +422,41 @@ static __device__ __forceinline__ void unit_prefetch(const TrackParams &P, int64
 // claims the CTA's next unit of the phase and issues that unit's first tiles, so that their
 // copies overlap this unit's reduction.  Returns the next unit (>= n_units: none), or -1 if a
 // TMA wait gave up (CCT_ERR_TIMEOUT recorded).
-// Small-batch schedule: unit u adds its field at particle pi into its copy of the fixed-point
-// accumulators of stage parity `parity` (a component out of range or non-finite counts on the
-// particle's flag instead).
-static __device__ __forceinline__ void tiny_add(const TrackParams &P, int64_t u, int parity, int64_t pi, double x,
-                                                double y, double z) {
+// round(x * 2^44) of an FP32 value by integer operations (no FP64 or 64-bit conversion: both
+// run at GB300's low FP64 rate), halves rounded away from zero; kTinyBad for |x| >= 2^18 T,
+// infinities and NaN.
+constexpr long long kTinyBad = (long long)0x8000000000000000ull;
+__device__ __forceinline__ long long fixed44(float x) {
+    const unsigned b = __float_as_uint(x);
+    const int e = (int)((b >> 23) & 0xffu);
+    if (e >= 127 + 18) return kTinyBad;
+    if (e == 0) return 0;                                   // zero, or below 2^-126
+    const long long m = (long long)((b & 0x7fffffu) | 0x800000u);
+    const int sh = e - 106;                                 // x 2^44 = m 2^(e - 127 - 23 + 44)
+    long long v = 0;
+    if (sh >= 0) v = m << sh;                               // < 2^24 2^38 = 2^62
+    else if (sh >= -24) v = (m + (1ll << (-sh - 1))) >> (-sh);
+    return (b >> 31) ? -v : v;
+}
+
+// A compensated FP32 pair (S, C) as fixed point: fixed44(S) - fixed44(C), or kTinyBad.
+__device__ __forceinline__ long long fixed44_pair(float S, float C) {
+    const long long a = fixed44(S), c = fixed44(C);
+    if (a == kTinyBad || c == kTinyBad) return kTinyBad;
+    return a - c;                                           // |a|, |c| < 2^62
+}
+
+// Small-batch schedule: unit u adds its field at particle pi, in fixed point, into its copy of
+// the accumulators of stage parity `parity` (kTinyBad components count on the particle's flag).
+static __device__ __forceinline__ void tiny_add_fixed(const TrackParams &P, int64_t u, int parity, int64_t pi,
+                                                      const long long (&v)[3]) {
     const int64_t total = (int64_t)P.n_designs * P.n_p;
     const int64_t slot = ((u % P.tiny_copies) * 2 + parity) * total + pi;
     unsigned long long *acc = reinterpret_cast<unsigned long long *>(P.tiny_acc + slot * 3);
-    const double v[3] = {x, y, z};
     bool bad = false;
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-        if (fabs(v[c]) < kTinyLimit) atomicAdd(acc + c, (unsigned long long)__double2ll_rn(v[c] * kTinyScale));
+        if (v[c] != kTinyBad) atomicAdd(acc + c, (unsigned long long)v[c]);
         else bad = true;
     }
     if (bad) atomicAdd(P.tiny_bad + slot, 1u);
@@ -465,9 +488,17 @@ static __device__ int64_t unit_sum_f32c(const TrackParams &P, const PointSrc &sr
         int64_t j = U.b * G + pl0 + i * 32;
         if (j >= P.n_p) j = P.n_p - 1;
         const int64_t pi = (int64_t)U.d * P.n_p + j;
-        const double *Ys = src.pos + pi * src.pos_stride;
+        if (TINY) {   // the CTA's own double-float copy of the position
 #pragma unroll
-        for (int c = 0; c < 3; ++c) split_df(Ys[c], ph[i][c], pl[i][c]);
+            for (int c = 0; c < 3; ++c) {
+                ph[i][c] = sm.tiny_pts[pi][c];
+                pl[i][c] = sm.tiny_pts[pi][3 + c];
+            }
+        } else {
+            const double *Ys = src.pos + pi * src.pos_stride;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) split_df(Ys[c], ph[i][c], pl[i][c]);
+        }
         if (GRAD) {
 #pragma unroll
             for (int c = 0; c < 3; ++c) a[i][c] = (float)src.w[pi * src.w_stride + c];
@@ -519,32 +550,48 @@ static __device__ int64_t unit_sum_f32c(const TrackParams &P, const PointSrc &sr
         if (next < n_units) unit_prefetch(P, next, sm, kt);
     }
 
-    // reduce the S slices of every particle in fixed order
+    if (TINY) {   // small batches: the slices' fields in fixed point, summed in integers
+        long long *ri = reinterpret_cast<long long *>(sm.red);
 #pragma unroll
-    for (int i = 0; i < PPT; ++i) {
-        double *r = sm.red + ((size_t)sl * G + pl0 + i * 32) * 3;
-        r[0] = acc.total(i, 0);
-        r[1] = acc.total(i, 1);
-        r[2] = acc.total(i, 2);
-    }
-    __syncthreads();
-    for (int slot = tid; slot < G; slot += kTrackBlock) {
-        double sx = 0.0, sy = 0.0, sz = 0.0;
-        for (int q = 0; q < S; ++q) {
-            const double *r = sm.red + ((size_t)q * G + slot) * 3;
-            sx += r[0];
-            sy += r[1];
-            sz += r[2];
-        }
-        if (TINY) {
+        for (int i = 0; i < PPT; ++i)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) ri[((size_t)sl * G + pl0 + i * 32) * 3 + c] = fixed44_pair(acc.S[i][c], acc.C[i][c]);
+        __syncthreads();
+        for (int slot = tid; slot < G; slot += kTrackBlock) {
+            long long v[3] = {0, 0, 0};
+            for (int q = 0; q < S; ++q)
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    const long long t = ri[((size_t)q * G + slot) * 3 + c];
+                    v[c] = (v[c] == kTinyBad || t == kTinyBad)
+                               ? kTinyBad
+                               : (long long)((unsigned long long)v[c] + (unsigned long long)t);
+                }
             const int64_t j = U.b * G + slot;
-            if (j < P.n_p) tiny_add(P, u, phase & 1, (int64_t)U.d * P.n_p + j, sx, sy, sz);
-            continue;
+            if (j < P.n_p) tiny_add_fixed(P, u, phase & 1, (int64_t)U.d * P.n_p + j, v);
         }
-        double *out = P.partial + (u * G + slot) * 3;
-        out[0] = sx;
-        out[1] = sy;
-        out[2] = sz;
+    } else {   // reduce the S slices of every particle in fixed order
+#pragma unroll
+        for (int i = 0; i < PPT; ++i) {
+            double *r = sm.red + ((size_t)sl * G + pl0 + i * 32) * 3;
+            r[0] = acc.total(i, 0);
+            r[1] = acc.total(i, 1);
+            r[2] = acc.total(i, 2);
+        }
+        __syncthreads();
+        for (int slot = tid; slot < G; slot += kTrackBlock) {
+            double sx = 0.0, sy = 0.0, sz = 0.0;
+            for (int q = 0; q < S; ++q) {
+                const double *r = sm.red + ((size_t)q * G + slot) * 3;
+                sx += r[0];
+                sy += r[1];
+                sz += r[2];
+            }
+            double *out = P.partial + (u * G + slot) * 3;
+            out[0] = sx;
+            out[1] = sy;
+            out[2] = sz;
+        }
     }
     __syncthreads();
     return next;
@@ -760,8 +807,11 @@ static __device__ void tiny_advance(const TrackParams &P, TrackSmem &sm, int ste
         }
         prev[3] = (long long)bad;
         double *S = sm.tiny_state + pi * kStateD;
-        if ((double)step < S[ST_NSTEPS])
+        if ((double)step < S[ST_NSTEPS]) {
             particle_update_at(P, S, pi, step, stage, B, sm.tiny_qs[pi][0], sm.tiny_qs[pi][1]);
+#pragma unroll
+            for (int c = 0; c < 3; ++c) split_df(S[ST_YS + c], sm.tiny_pts[pi][c], sm.tiny_pts[pi][3 + c]);
+        }
     }
 }
 
