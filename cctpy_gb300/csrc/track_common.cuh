@@ -53,8 +53,10 @@ constexpr int kCtrlTinyCount = kCtrlLineWords;          // word index of the fir
 // units' atomic additions spread over more addresses; readers add the copies up.
 constexpr int kTinyMax = 64;
 constexpr int kTinyCopies = 8;    // measured on C0 (32 protons): 2 -> 12.5, 4 -> 10.0, 8 -> 9.1, 12 -> 9.9, 16 -> 10.1 us a stage
-constexpr double kTinyScale = 17592186044416.0;        // 2^44: 5.7e-14 T resolution
-constexpr double kTinyLimit = 262144.0;                 // 2^18 T: far inside the int64 range
+constexpr int kTinyShift = 44;                          // fixed point: 2^-44 T, 5.7e-14 T resolution
+constexpr double kTinyScale = 17592186044416.0;        // 2^kTinyShift
+constexpr int kTinyRange = 18;                          // unit fields below 2^18 T: far inside int64
+static_assert(kTinyShift + kTinyRange + 1 <= 63, "fixed-point fields (< 2^62) and their differences fit int64");
 
 // Dataflow schedule (batches of at least kFlowMinBlocks particle blocks): per particle block a
 // 64-bit count of finished chunk units and a 32-bit count of finished stages.
@@ -422,17 +424,17 @@ static __device__ __forceinline__ void unit_prefetch(const TrackParams &P, int64
 // claims the CTA's next unit of the phase and issues that unit's first tiles, so that their
 // copies overlap this unit's reduction.  Returns the next unit (>= n_units: none), or -1 if a
 // TMA wait gave up (CCT_ERR_TIMEOUT recorded).
-// round(x * 2^44) of an FP32 value by integer operations (no FP64 or 64-bit conversion: both
-// run at GB300's low FP64 rate), halves rounded away from zero; kTinyBad for |x| >= 2^18 T,
-// infinities and NaN.
+// round(x * 2^kTinyShift) of an FP32 value by integer operations (no FP64 or 64-bit
+// conversion: both run at GB300's low FP64 rate), halves rounded away from zero; kTinyBad for
+// |x| >= 2^kTinyRange T, infinities and NaN.
 constexpr long long kTinyBad = (long long)0x8000000000000000ull;
 __device__ __forceinline__ long long fixed44(float x) {
     const unsigned b = __float_as_uint(x);
     const int e = (int)((b >> 23) & 0xffu);
-    if (e >= 127 + 18) return kTinyBad;
+    if (e >= 127 + kTinyRange) return kTinyBad;
     if (e == 0) return 0;                                   // zero, or below 2^-126
     const long long m = (long long)((b & 0x7fffffu) | 0x800000u);
-    const int sh = e - 106;                                 // x 2^44 = m 2^(e - 127 - 23 + 44)
+    const int sh = e - (127 + 23 - kTinyShift);            // x 2^44 = m 2^(e - 127 - 23 + 44)
     long long v = 0;
     if (sh >= 0) v = m << sh;                               // < 2^24 2^38 = 2^62
     else if (sh >= -24) v = (m + (1ll << (-sh - 1))) >> (-sh);
