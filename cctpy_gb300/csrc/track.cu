@@ -73,6 +73,7 @@ static __device__ bool flow_f32c(const TrackParams &P, TrackSmem &sm, uint32_t &
 }
 
 // The same for FP64 units (no tile ring).
+template <bool HALF = false>
 static __device__ bool flow_f64(const TrackParams &P, TrackSmem &sm, int64_t n_units, int64_t n_seq) {
     for (int64_t s = first_unit(); s < n_seq; s = claim_seq(P, sm)) {
         const int k = (int)(s / n_units);
@@ -80,7 +81,7 @@ static __device__ bool flow_f64(const TrackParams &P, TrackSmem &sm, int64_t n_u
         const UnitRef U = locate_unit(P, u);
         const int64_t blk = (int64_t)U.d * P.blocks + U.b;
         if (!flow_wait(P, sm, blk, k)) return false;
-        unit_field_f64(P, u, sm);
+        unit_field_f64<HALF>(P, u, sm);
         if (flow_complete(P, sm, blk, k, P.chunks[U.d])) block_update(P, U.d, U.b, k);
     }
     return true;
@@ -231,7 +232,8 @@ __global__ void __launch_bounds__(kTrackBlock, kTrackMinBlocks) track_kernel(Tra
 
     if (P.use_flow) {
         const int64_t n_seq = step_end > P.step_begin ? (int64_t)(step_end - P.step_begin) * 4 * n_units : 0;
-        if (P.precision == 0) (void)flow_f64(P, sm, n_units, n_seq);
+        if (P.precision == 0 && P.G == kHalfGroup) (void)flow_f64<true>(P, sm, n_units, n_seq);
+        else if (P.precision == 0) (void)flow_f64(P, sm, n_units, n_seq);
         else if (P.G == kHalfGroup) (void)flow_f32c<1, true>(P, sm, kt, n_units, n_seq);
         else if (P.ppt == 2) (void)flow_f32c<2>(P, sm, kt, n_units, n_seq);
         else (void)flow_f32c<1>(P, sm, kt, n_units, n_seq);
@@ -241,8 +243,10 @@ __global__ void __launch_bounds__(kTrackBlock, kTrackMinBlocks) track_kernel(Tra
     for (int step = P.step_begin; !P.use_flow && step < step_end; ++step) {
         for (int stage = 0; stage < 4; ++stage, ++phase) {
             if (P.precision == 0) {
-                for (int64_t u = first_unit(); u < n_units; u = next_unit(P, sm, phase))
-                    unit_field_f64(P, u, sm);
+                for (int64_t u = first_unit(); u < n_units; u = next_unit(P, sm, phase)) {
+                    if (P.G == kHalfGroup) unit_field_f64<true>(P, u, sm);
+                    else unit_field_f64(P, u, sm);
+                }
             } else if (P.G == kHalfGroup) {
                 units_f32c<1, false, true>(P, stage_points(P), sm, kt, phase, n_units);
             } else if (P.ppt == 2) {
@@ -315,11 +319,11 @@ TrackScratchLayout track_scratch_layout(int n_designs, int64_t n_particles, int6
 // Particles per unit: FP64 keeps 32 (warps split the tiles); FP32c takes the block size that
 // needs the fewest particle slots (blocks x G), the largest of those: e.g. 100 particles run as
 // one block of 128 rather than two of 64 (the same slots), 96 as three blocks of 32.
-// min_group 16 (the forward's FP32c tracking) also allows half-warp blocks of 16, for designs
-// of at most 16 particles.
+// min_group 16 (the forward tracking, both precisions) also allows half-warp blocks of 16, for
+// designs of at most 16 particles.
 int group_size(int precision, int64_t n_p, int min_group) {
-    if (precision == 0) return 32;
     if (min_group <= kHalfGroup && n_p <= kHalfGroup) return kHalfGroup;
+    if (precision == 0) return 32;
     int best = kMaxGroup;
     int64_t best_slots = (n_p + best - 1) / best * best;
     for (int G = kMaxGroup / 2; G >= 32; G /= 2) {

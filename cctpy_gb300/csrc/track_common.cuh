@@ -318,10 +318,18 @@ __device__ __forceinline__ UnitRef locate_unit(const TrackParams &P, int64_t u) 
 // m = kl x (p0 - o) about the tile's first midpoint o, then the group's segments are broadcast
 // lane to lane and every lane sums A = sum kl |r|^-3, M = sum m |r|^-3 for its particle; the
 // tile's field is A x (p - o) - M (the moment form of the field kernel, in FP64).
+// HALF: blocks of kHalfGroup particles: lanes l and l + 16 hold particle l and sum the first
+// and the second 16 segments of each group of 32 (an FP64 warp instruction costs the same
+// with half its lanes idle, so designs of at most 16 particles would otherwise run at half
+// rate); the halves are added lane l + 16 into lane l before the CTA reduction.
+template <bool HALF = false>
 static __device__ void unit_field_f64(const TrackParams &P, int64_t u, TrackSmem &sm) {
     const UnitRef U = locate_unit(P, u);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    int64_t j = U.b * 32 + lane;
+    constexpr int G = HALF ? kHalfGroup : 32;
+    constexpr int KN = HALF ? 16 : 32;                 // segments of a group summed by a lane
+    const int pl = HALF ? (lane & 15) : lane, k0 = HALF ? (lane & 16) : 0;
+    int64_t j = U.b * G + pl;
     if (j >= P.n_p) j = P.n_p - 1;
     const double *Ys = P.state + ((int64_t)U.d * P.n_p + j) * kStateD + ST_YS;
     const double px = Ys[0], py = Ys[1], pz = Ys[2];
@@ -344,8 +352,11 @@ static __device__ void unit_field_f64(const TrackParams &P, int64_t u, TrackSmem
                 qz = __ldg(P.p0s + 3 * s + 2) - oz;
             }
             const double mx = ky * qz - kz * qy, my = kz * qx - kx * qz, mz = kx * qy - ky * qx;
-            const int n = (int)min((int64_t)32, e - g);
-            for (int k = 0; k < n; ++k) {
+            // past the tile's end a lane holds kl = 0 far away, whose terms are exactly zero:
+            // half-warps run all 16 of theirs (a warp-uniform count for the shuffles)
+            const int n = HALF ? KN : (int)min((int64_t)32, e - g);
+            for (int kk = 0; kk < n; ++kk) {
+                const int k = k0 + kk;
                 const double skx = __shfl_sync(0xffffffffu, kx, k), sky = __shfl_sync(0xffffffffu, ky, k),
                              skz = __shfl_sync(0xffffffffu, kz, k);
                 const double sqx = __shfl_sync(0xffffffffu, qx, k), sqy = __shfl_sync(0xffffffffu, qy, k),
@@ -367,20 +378,27 @@ static __device__ void unit_field_f64(const TrackParams &P, int64_t u, TrackSmem
         by += (Az * wx - Ax * wz) - My;
         bz += (Ax * wy - Ay * wx) - Mz;
     }
-    double *red = sm.red + (warp * 32 + lane) * 3;
-    red[0] = bx;
-    red[1] = by;
-    red[2] = bz;
+    if (HALF) {
+        bx += __shfl_down_sync(0xffffffffu, bx, 16);
+        by += __shfl_down_sync(0xffffffffu, by, 16);
+        bz += __shfl_down_sync(0xffffffffu, bz, 16);
+    }
+    double *red = sm.red + (warp * G + pl) * 3;
+    if (lane < G) {
+        red[0] = bx;
+        red[1] = by;
+        red[2] = bz;
+    }
     __syncthreads();
-    if (warp == 0) {
+    if (warp == 0 && lane < G) {
         double sx = 0.0, sy = 0.0, sz = 0.0;
         for (int w = 0; w < kTrackWarps; ++w) {
-            const double *r = sm.red + (w * 32 + lane) * 3;
+            const double *r = sm.red + (w * G + lane) * 3;
             sx += r[0];
             sy += r[1];
             sz += r[2];
         }
-        double *out = P.partial + (u * 32 + lane) * 3;
+        double *out = P.partial + (u * G + lane) * 3;
         out[0] = sx;
         out[1] = sy;
         out[2] = sz;

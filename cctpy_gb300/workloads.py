@@ -146,6 +146,22 @@ def build_gantry_section(**overrides):
     return HUST_SC_GANTRY(**kw).create_second_bending_part_beamline()
 
 
+def build_speed_test_beamline(currents=(10000.0, 10000.0)):
+    """The beamline of cctpy's GPU speed test (final_code/work/小论文2回复/CPU和CPU代码速度测试.py:
+    36-52): a 5 m drift, an AG-CCT (bending radius 1 m, aperture radii 200/180/160/140 mm,
+    bends 10/10/15/15 deg, tilts [30] and [90, 30], 50 and 10/10/15/15 turns, 10 kA each),
+    a 2 m drift, a 1 m QS of zero gradients (200 mm aperture) and a 2 m drift: 24 000
+    segments, 10.8727 m.  ``currents``: the dipole and AG layers' currents (A)."""
+    from .beamline import Beamline
+    from .geometry import P2
+    return (Beamline.set_start_point(P2.origin()).first_drift(direct=P2.x_direct(), length=5)
+            .append_agcct(big_r=1.0, small_rs=[200 * MM, 180 * MM, 160 * MM, 140 * MM],
+                          bending_angles=[10, 10, 15, 15], tilt_angles=[[30], [90, 30]],
+                          winding_numbers=[[50], [10, 10, 15, 15]], currents=[float(c) for c in currents])
+            .append_drift(2).append_qs(length=1, gradient=0, second_gradient=0, aperture_radius=200 * MM)
+            .append_drift(2))
+
+
 def beam_particles(bl, n: int, seed: int, kinetic_MeV: float, gaussian: bool = True) -> np.ndarray:
     """(n, 10) proton records at the start of beamline `bl`."""
     from .particles import ParticleFactory, PhaseSpaceParticle, particles_to_array

@@ -1,0 +1,74 @@
+"""The engine beside cctpy's own CUDA tracking kernel on the same GPU and the same inputs.
+
+cctpy's GPU path (final_code/packages/gpu_accelerator.py:100-1078, launched at :1931-2031) is
+compiled for this device from cctpy's own source by ``oracle/ref_cuda_build.py`` (at build
+time, where the cctpy sources are) and launched unmodified by ``oracle/ref_cuda.py``: one
+block per beamline, particles one after another, every field a block-wide strided sum and
+tree reduction.  Two beamlines of the reference's GPU speed test (the second with other
+AG-CCT currents, so that a design mix-up shows) carry four 250 MeV protons through the
+entrance of the AG-CCT.
+
+* FP64: cctpy's FLOAT64 kernel and the engine's FP64 path agree to rounding: their field sums
+  differ only in summation order.
+* FP32: cctpy's FLOAT32 kernel (its speed-test configuration) is several orders of magnitude
+  further from the FP64 track than the engine's FP32-compensated path.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+S0, LENGTH, STEP = 4.9, 1.2, 0.01      # m: from the end of the entrance drift into the AG-CCT
+N_P = 4
+
+
+def _setup():
+    from oracle import ref_cuda
+    if not ref_cuda.available():
+        pytest.skip("cctpy's CUDA kernels were not built (oracle/ref_cuda_build.py needs cctpy's sources)")
+    from cctpy_gb300 import engine, workloads as W
+    from cctpy_gb300.particles import ParticleFactory, PhaseSpaceParticle, particles_to_array
+    a = W.build_speed_test_beamline()
+    b = W.build_speed_test_beamline(currents=(8000.0, 12000.0))
+    ideal = ParticleFactory.create_proton_along(a, S0, 250.0)
+    pss = W.gaussian_phase_space(N_P, seed=11)
+    ps = particles_to_array(ParticleFactory.create_from_phase_space_particles(
+        ideal, ideal.get_natural_coordinate_system(), [PhaseSpaceParticle(*map(float, r)) for r in pss]))
+    designs = [engine.host_design(engine.magnet_list(bl)) for bl in (a, b)]
+    return ref_cuda, engine, designs, ps
+
+
+def test_fp64_matches_cctpy_cuda_kernel():
+    ref_cuda, engine, designs, ps = _setup()
+    ref = ref_cuda.ReferenceCudaTracker("f64")
+    try:
+        want, _, _ = ref.track(designs, ps, LENGTH, STEP)
+    finally:
+        ref.close()
+    ds = engine.DesignSet(designs)
+    got = engine.track(ds, ps, LENGTH, STEP, "f64")
+    assert got.shape == want.shape == (2, N_P, 10)
+    # the two designs really differ at this tolerance
+    assert np.abs(want[0, :, :3] - want[1, :, :3]).max() > 1e-6
+    pos = np.abs(got[:, :, :3] - want[:, :, :3]).max()
+    vel = (np.abs(got[:, :, 3:6] - want[:, :, 3:6]) / np.abs(want[:, :, 3:6]).max()).max()
+    assert pos < 1e-12, f"FP64 positions differ from cctpy's CUDA kernel by {pos:.3e} m"
+    assert vel < 1e-12, f"FP64 velocities differ from cctpy's CUDA kernel by {vel:.3e} (relative)"
+
+
+def test_fp32c_closer_to_fp64_than_cctpy_fp32_kernel():
+    ref_cuda, engine, designs, ps = _setup()
+    ds = engine.DesignSet(designs)
+    truth = engine.track(ds, ps, LENGTH, STEP, "f64")
+    ours = engine.track(ds, ps, LENGTH, STEP, "f32c")
+    ref = ref_cuda.ReferenceCudaTracker("f32")
+    try:
+        theirs, _, _ = ref.track(designs, ps, LENGTH, STEP)
+    finally:
+        ref.close()
+    err_ours = np.abs(ours[:, :, :3] - truth[:, :, :3]).max()
+    err_ref = np.abs(theirs[:, :, :3] - truth[:, :, :3]).max()
+    assert err_ours < 1e-6, f"FP32c position error {err_ours:.3e} m"
+    assert err_ours * 10 < err_ref, f"FP32c {err_ours:.3e} m against cctpy's FLOAT32 kernel {err_ref:.3e} m"
+    # the reference's FP32 kernel still tracks the same beam (its documented error: ~0.05 mm)
+    assert err_ref < 1e-3

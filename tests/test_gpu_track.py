@@ -218,6 +218,25 @@ def test_half_warp_blocks_of_16_protons(golden, n_designs):
         assert np.abs(out[d][:, 0:3] - f64[:, 0:3]).max() < POS_TOL_F32C
 
 
+@pytest.mark.parametrize("n_designs", [1, 9])
+def test_fp64_half_warp_blocks_of_16_protons(golden, n_designs):
+    """FP64 designs of 16 protons run in blocks of 16 too (lanes l and l + 16 hold proton l
+    and sum the two halves of every 32-segment group): one design on grid barriers, nine on
+    the dataflow schedule.  Every copy tracks the reference's protons at the FP64 bar, and
+    agrees with the same protons in a block of 32 (a 17th proton added) to rounding."""
+    _, cct = W.build_single_dipole()
+    parts = golden["sd_particles_in"][:16]
+    L = W.single_dipole_track_length()
+    ds = engine.design_set_of([cct] * n_designs)
+    out = engine.track(ds, np.stack([parts] * n_designs), L, 0.001, "f64")
+    blk32 = engine.track(engine.design_of(cct), golden["sd_particles_in"][:17], L, 0.001, "f64")[0][:16]
+    for d in range(n_designs):
+        check(out[d], golden["sd_particles_out"][:16], POS_TOL_F64, VEL_RTOL_F64)
+        np.testing.assert_array_equal(out[d], out[0])
+        assert np.abs(out[d][:, 0:3] - blk32[:, 0:3]).max() < 1e-12
+        assert (np.abs(out[d][:, 3:6] - blk32[:, 3:6]) / np.abs(blk32[:, 3:6]).max()).max() < 1e-12
+
+
 def test_bounded_small_batch_wait_reports_timeout(golden):
     """A small FP32c batch (the small-batch schedule: CTAs wait on unit counters between
     stages); the test hook makes every such wait ask for a stage more than exists: it gives

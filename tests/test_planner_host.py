@@ -40,10 +40,10 @@ def plan(lib, seg_counts, n_p, precision, grid, max_units=0):
 
 
 def expected_group(precision, n_p):
+    if n_p <= 16:              # half-warp blocks for designs of at most 16 particles
+        return 16
     if precision == 0:
         return 32
-    if n_p <= 16:              # FP32c: half-warp blocks for designs of at most 16 particles
-        return 16
     best, slots = 256, -(-n_p // 256) * 256
     for G in (128, 64, 32):
         s = -(-n_p // G) * G
@@ -204,12 +204,12 @@ def test_small_fp32c_batches_plan_one_unit_per_cta(lib):
 
 
 def test_half_warp_blocks_for_designs_of_up_to_16_particles(lib):
-    """FP32c designs of at most 16 particles get blocks of 16 (a particle per half-warp lane,
-    so that no lane idles); 17 particles and FP64 keep blocks of 32; the adjoint's scratch
-    query stays on blocks of 32 or more."""
+    """Designs of at most 16 particles get blocks of 16 in both precisions (a particle per
+    half-warp lane, so that no lane idles); 17 particles keep blocks of 32."""
     for n_p in (1, 5, 16):
         assert plan(lib, [24000] * 100, n_p, 1, 456)[4] == 16
-        assert plan(lib, [24000] * 100, n_p, 0, 456)[4] == 32
+        assert plan(lib, [24000] * 100, n_p, 0, 456)[4] == 16
     assert plan(lib, [24000] * 100, 17, 1, 456)[4] == 32
+    assert plan(lib, [24000] * 100, 17, 0, 456)[4] == 32
     units, unit_off, chunks, ct, g = plan(lib, [24000] * 100, 16, 1, 456)
     assert units == unit_off[-1] and np.all(unit_off[1:] - unit_off[:-1] == chunks)
