@@ -598,6 +598,60 @@ def measure_cpu_baselines(args, ds):
     return cpu, cpu_track, acc
 
 
+def measure_reference_gpu_baseline():
+    """cctpy's own CUDA tracking kernel on this GPU, beside the engine on the same inputs: the
+    workload of cctpy's GPU speed test (100 copies of its 24 000-segment AG-CCT beamline, 16
+    copies of the ideal 250 MeV proton each, 20 mm RK4 step).  FLOAT32 (1024 threads a block,
+    the speed test's configuration) over the whole 10.87 m; FLOAT64 (512 threads) over 1/32 of
+    it (0.34 m) from 4.9 m on the design orbit, into the AG-CCT.  cctpy's kernel source (final_code/packages/gpu_accelerator.py:100-1078)
+    is compiled for sm_103a from cctpy's tree at build time (oracle/ref_cuda_build.py) and
+    launched as cctpy's host code does (gpu_accelerator.py:1931-2031; oracle/ref_cuda.py);
+    its per-call JIT compile is left out.  "call" times include cctpy's array packing (segment
+    arrays padded to its capacities) and its copies; ours are engine.track with the same host
+    particle records in and out."""
+    import torch
+    from oracle import ref_cuda
+    if not ref_cuda.available():
+        return {"unavailable": "cctpy's CUDA kernels were not built (oracle/ref_cuda_build.py needs cctpy's "
+                               "sources at build time)"}
+    from cctpy_gb300 import engine, workloads as W
+    from cctpy_gb300.particles import ParticleFactory, particles_to_array
+    bl = W.build_speed_test_beamline()
+    L = bl.get_length()
+    design = engine.host_design(engine.magnet_list(bl))
+    n_seg = design[0].shape[0]
+    starts = {"f32": 0.0, "f64": 4.9}
+    designs = [design] * 100
+    ds = engine.DesignSet(designs)
+    out = {"kernel": "cctpy track_multi_particle_beamline_for_magnet_with_multi_qs, compiled from its source "
+                     "for sm_103a, one block per beamline",
+           "workload": f"100 beamlines x {n_seg} segments (cctpy's GPU speed test), 16 protons each, 20 mm step"}
+    for prec, ours_prec, frac in (("f32", "f32c", 1.0), ("f64", "f64", 1.0 / 32)):
+        ps = particles_to_array([ParticleFactory.create_proton_along(bl, starts[prec])] * 16)
+        ref = ref_cuda.ReferenceCudaTracker(prec)
+        try:
+            ref.track(designs[:2], ps, 0.04, 0.02)                              # module loaded, warm
+            dist = L * frac
+            theirs, k_s, call_s = ref.track(designs, ps, dist, 0.02)
+        finally:
+            ref.close()
+        engine.track(ds, ps, 0.04, 0.02, ours_prec)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        mine = engine.track(ds, ps, dist, 0.02, ours_prec)
+        torch.cuda.synchronize()
+        ours_s = time.perf_counter() - t0
+        steps = int(np.ceil(dist / 0.02))
+        pairs = 100 * 16 * steps * 4 * n_seg
+        out[prec] = {"start_m": starts[prec], "length_m": dist, "steps": steps, "block": ref.block,
+                     "kernel_seconds": k_s,
+                     "call_seconds": call_s, "gpairs_per_s": pairs / k_s / 1e9,
+                     f"ours_{ours_prec}_seconds": ours_s, "ours_gpairs_per_s": pairs / ours_s / 1e9,
+                     "ours_over_reference_kernel": k_s / ours_s, "ours_over_reference_call": call_s / ours_s,
+                     f"max_pos_diff_m_vs_ours_{ours_prec}": float(np.abs(theirs[:, :, :3] - mine[:, :, :3]).max())}
+    return out
+
+
 # ---------------------------------------------------------------- GPU arm
 def run_ours(args):
     import torch
@@ -732,9 +786,14 @@ def run_ours(args):
 
     line = None
     if rank == 0:
-        cpu = cpu_track = acc_oracle = None
+        cpu = cpu_track = acc_oracle = ref_gpu = None
         if world == 1 and not args.no_cpu_baseline:
             cpu, cpu_track, acc_oracle = measure_cpu_baselines(args, ds)
+            if not (args.no_tracking or args.no_speed_test):
+                try:
+                    ref_gpu = measure_reference_gpu_baseline()
+                except Exception as e:   # the headline line is printed whatever happens to this leg
+                    ref_gpu = {"error": f"{type(e).__name__}: {e}"[:300]}
         line = {
             "metric": METRIC, "value": value, "unit": "Gpairs/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
@@ -771,6 +830,7 @@ def run_ours(args):
             "tracking": tracking,
             "population_shard": shard,
             "cpu_baseline_tracking": cpu_track,
+            "reference_gpu_baseline": ref_gpu,
             "gpu_launches": args.steps,
             "clocks": clocks,
             "cpu_baseline": cpu,

@@ -52,6 +52,38 @@ class _Driver:
             raise RuntimeError(f"{what} failed: {name.value.decode() if name.value else rc}")
 
 
+def pack(designs, particles: np.ndarray, max_ce: int, max_qs: int, dtype) -> dict:
+    """Host arrays in cctpy's GPU layout (gpu_accelerator.py:1953-2016).  ``designs``: per
+    beamline (kls (n, 3), p0s (n, 3), qs (k, 16)); ``particles``: (n_p, 10) records, given to
+    every beamline; ``max_ce`` / ``max_qs``: the kernel's compiled capacities."""
+    D = len(designs)
+    parts = np.ascontiguousarray(particles, dtype=np.float64).reshape(-1, 10)
+    n_p = parts.shape[0]
+    if D < 1 or n_p < 1:
+        raise ValueError("need at least one beamline and one particle")
+    kls = np.zeros((D, 3 * max_ce), dtype)
+    p0s = np.zeros((D, 3 * max_ce), dtype)
+    qs = np.zeros((D, 16 * max_qs), dtype)
+    n_ce = np.zeros(D, np.int32)
+    n_qs = np.zeros(D, np.int32)
+    for d, (k, p, q) in enumerate(designs):
+        k = np.asarray(k, np.float64).reshape(-1)
+        p = np.asarray(p, np.float64).reshape(-1)
+        q = np.asarray(q, np.float64).reshape(-1)
+        if k.size % 3 or k.size != p.size or q.size % 16:
+            raise ValueError(f"beamline {d}: kls and p0s must be (n, 3) alike and QS records 16 doubles")
+        if k.size > 3 * max_ce or q.size > 16 * max_qs:
+            raise ValueError(f"beamline {d} exceeds cctpy's GPU capacities ({max_ce} current elements, "
+                             f"{max_qs} QS)")
+        kls[d, :k.size] = k
+        p0s[d, :p.size] = p
+        qs[d, :q.size] = q
+        n_ce[d] = k.size // 3
+        n_qs[d] = q.size // 16
+    return dict(kls=kls, p0s=p0s, n_ce=n_ce, qs=qs, n_qs=n_qs,
+                particles=np.tile(parts, (D, 1)).astype(dtype), n_p=np.array([n_p], np.int32))
+
+
 class ReferenceCudaTracker:
     """cctpy's GPU tracking kernel in one precision ("f32": FLOAT32 x 1024 threads, "f64":
     FLOAT64 x 512 threads), loaded on the current CUDA device."""
@@ -83,32 +115,8 @@ class ReferenceCudaTracker:
             self.drv.lib.cuModuleUnload(self.module)
             self.module = ctypes.c_void_p()
 
-    def pack(self, designs, particles: np.ndarray):
-        """Host arrays in cctpy's GPU layout (gpu_accelerator.py:1953-2016).  ``designs``: per
-        beamline (kls (n, 3), p0s (n, 3), qs (k, 16)); ``particles``: (n_p, 10) records."""
-        D = len(designs)
-        parts = np.ascontiguousarray(particles, dtype=np.float64).reshape(-1, 10)
-        n_p = parts.shape[0]
-        if D < 1 or n_p < 1:
-            raise ValueError("need at least one beamline and one particle")
-        kls = np.zeros((D, 3 * self.max_ce), self.np_dtype)
-        p0s = np.zeros((D, 3 * self.max_ce), self.np_dtype)
-        qs = np.zeros((D, 16 * self.max_qs), self.np_dtype)
-        n_ce = np.zeros(D, np.int32)
-        n_qs = np.zeros(D, np.int32)
-        for d, (k, p, q) in enumerate(designs):
-            k = np.asarray(k, np.float64).reshape(-1)
-            q = np.asarray(q, np.float64).reshape(-1)
-            if k.size > 3 * self.max_ce or q.size > 16 * self.max_qs:
-                raise ValueError(f"beamline {d} exceeds cctpy's GPU capacities "
-                                 f"({self.max_ce} current elements, {self.max_qs} QS)")
-            kls[d, :k.size] = k
-            p0s[d, :k.size] = np.asarray(p, np.float64).reshape(-1)
-            qs[d, :q.size] = q
-            n_ce[d] = k.size // 3
-            n_qs[d] = q.size // 16
-        return dict(kls=kls, p0s=p0s, n_ce=n_ce, qs=qs, n_qs=n_qs,
-                    particles=np.tile(parts, (D, 1)).astype(self.np_dtype), n_p=np.array([n_p], np.int32))
+    def pack(self, designs, particles: np.ndarray) -> dict:
+        return pack(designs, particles, self.max_ce, self.max_qs, self.np_dtype)
 
     def upload(self, host: dict, distance: float, footstep: float) -> dict:
         import torch

@@ -67,12 +67,20 @@ def cuda_sources(ref_dir: str) -> dict:
     return out
 
 
-def build(ref_dir: str, nvcc: str = "nvcc") -> dict:
+def build(ref_dir: str, nvcc: str = "nvcc", force: bool = False) -> dict:
+    """Compile both configurations (skipped when the cubins of this exact source are there)."""
     src_file = os.path.join(ref_dir, "final_code", "packages", "gpu_accelerator.py")
     if not os.path.isfile(src_file):
         raise FileNotFoundError(f"no cctpy GPU module at {src_file}")
     with open(src_file, "rb") as f:
         sha = hashlib.sha256(f.read()).hexdigest()
+    if not force and os.path.isfile(META):
+        with open(META) as f:
+            old = json.load(f)
+        if old.get("source_sha256") == sha and all(
+                os.path.isfile(os.path.join(OUT, c["cubin"])) for c in old.get("configs", {}).values()) \
+                and set(old.get("configs", {})) == {c[0] for c in CONFIGS}:
+            return old
     os.makedirs(OUT, exist_ok=True)
     meta = {"kernel": KERNEL, "source": "final_code/packages/gpu_accelerator.py", "source_sha256": sha,
             "arch": "sm_103a", "configs": {}}
