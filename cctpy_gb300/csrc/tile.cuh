@@ -130,20 +130,18 @@ __device__ __forceinline__ void tile_offsets(const TileHeader *h, const float (&
         }
 }
 
-// SLG: 4-segment groups a slice covers within a sub-block (kSub / 4 = a whole sub-block; half
-// of it for the 16-particle blocks, whose half-warps take half sub-blocks).  g0 and g1 are
-// multiples of SLG.
-template <int PPT, int JU, bool RCP, int SLG>
+// g0 and g1 are multiples of kSub / 4 (whole sub-blocks).
+template <int PPT, int JU, bool RCP>
 __device__ __forceinline__ void tile_pairs(const unsigned char *tile, const f2 (&q)[PPT][3], F32cAcc<PPT> &acc,
                                            int g0, int g1);
 
-template <int PPT, int JU = 1, bool RCP = false, int SLG = kSub / 4>
+template <int PPT, int JU = 1, bool RCP = false>
 __device__ __forceinline__ void tile_f32c(const unsigned char *tile, const float (&ph)[PPT][3],
                                           const float (&pl)[PPT][3], F32cAcc<PPT> &acc, int g0 = 0,
                                           int g1 = kTile / 4) {
     f2 q[PPT][3];
     tile_offsets<PPT>(reinterpret_cast<const TileHeader *>(tile), ph, pl, q);
-    tile_pairs<PPT, JU, RCP, SLG>(tile, q, acc, g0, g1);
+    tile_pairs<PPT, JU, RCP>(tile, q, acc, g0, g1);
 }
 
 // The same with the point's double-float coordinates kept in shared memory: component c
@@ -162,20 +160,18 @@ __device__ __forceinline__ void tile_f32c_smem(const unsigned char *tile, const 
         }
     f2 q[PPT][3];
     tile_offsets<PPT>(reinterpret_cast<const TileHeader *>(tile), ph, pl, q);
-    tile_pairs<PPT, JU, RCP, kSub / 4>(tile, q, acc, g0, g1);
+    tile_pairs<PPT, JU, RCP>(tile, q, acc, g0, g1);
 }
 
-template <int PPT, int JU, bool RCP, int SLG>
+template <int PPT, int JU, bool RCP>
 __device__ __forceinline__ void tile_pairs(const unsigned char *tile, const f2 (&q)[PPT][3], F32cAcc<PPT> &acc,
                                            int g0, int g1) {
     const TileHeader *h = reinterpret_cast<const TileHeader *>(tile);
     const ulonglong2 *v = reinterpret_cast<const ulonglong2 *>(tile + kTileHeaderBytes);
     constexpr int Q = kTile / 4;          // ulonglong2 (4 floats) per component array
     constexpr int SG = kSub / 4;          // 4-segment groups per sub-block
-    static_assert(SG % SLG == 0, "slices hold whole parts of one sub-block");
-    // g0 and g1 are multiples of SLG (whole sub-blocks, or halves).  T collects the slices' A x w
-    // (A summed over a slice of a sub-block, w = q - that sub-block's origin: the moment form
-    // holds for any set of segments about one origin); the moments M of the call are summed
+    // g0 and g1 are multiples of SG (whole sub-blocks).  T collects the sub-blocks' A x w
+    // (A summed over a sub-block, w = q - that sub-block's origin); the moments M of the call are summed
     // together and subtracted once.
     float T[PPT][3];
     f2 M[PPT][3];
@@ -187,12 +183,12 @@ __device__ __forceinline__ void tile_pairs(const unsigned char *tile, const f2 (
             M[i][c] = 0ull;
         }
 #pragma unroll 1
-    for (int sb = g0; sb < g1; sb += SLG) {
+    for (int sb = g0; sb < g1; sb += SG) {
         f2 A[PPT][3];
 #pragma unroll
         for (int i = 0; i < PPT; ++i) A[i][0] = A[i][1] = A[i][2] = 0ull;
 #pragma unroll JU
-        for (int j = sb; j < sb + SLG; ++j) {                    // 4 segments per iteration
+        for (int j = sb; j < sb + SG; ++j) {                     // 4 segments per iteration
             const ulonglong2 KX = v[0 * Q + j], KY = v[1 * Q + j], KZ = v[2 * Q + j];
             const ulonglong2 MX = v[3 * Q + j], MY = v[4 * Q + j], MZ = v[5 * Q + j];
             const ulonglong2 PX = v[6 * Q + j], PY = v[7 * Q + j], PZ = v[8 * Q + j];

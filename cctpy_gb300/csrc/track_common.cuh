@@ -485,8 +485,11 @@ static __device__ __forceinline__ void tiny_add_fixed(const TrackParams &P, int6
 // (TINY: the unit's reduced field goes to the small-batch accumulators; resident: the unit's
 // nt <= kRing tiles already sit in ring slots 0..nt-1 from an earlier stage of this CTA's only
 // unit; known: the unit's description, if the caller has it.)
-// HALF: blocks of kHalfGroup particles (PPT 1): lanes l and l + 16 of a warp hold particle l,
-// the two half-warps take different 16-segment halves of a sub-block (8 slices of each tile).
+// HALF: blocks of kHalfGroup particles (PPT 1): lanes l and l + 16 of a warp hold particle l.
+// A tile is shared by a pair of warps (warps 0-1 take the even tiles, 2-3 the odd ones), each
+// half-warp summing one whole 32-segment sub-block of it, so that the per-tile work of a
+// thread (offsets from the tile origin, the sub-block epilogue, the compensated add) covers
+// 32 segments rather than 16.
 template <int PPT, bool GRAD, bool FLOW = false, bool TINY = false, bool HALF = false>
 static __device__ int64_t unit_sum_f32c(const TrackParams &P, const PointSrc &src, int64_t u, TrackSmem &sm,
                                         uint32_t &kt, int phase, int64_t n_units, int64_t n_seq = 0,
@@ -500,7 +503,12 @@ static __device__ int64_t unit_sum_f32c(const TrackParams &P, const PointSrc &sr
     const int sb = HALF ? 0 : warp % NB;
     const int sl = HALF ? 2 * warp + (lane >> 4) : warp / NB;
     const int pl0 = HALF ? (lane & 15) : sb * 32 * PPT + lane;       // this lane's first particle slot
-    const int g0 = sl * (kTile / 4 / S), g1 = g0 + kTile / 4 / S;
+    constexpr int TW = HALF ? kTrackWarps / 2 : 1;                  // tiles in flight across the warps
+    constexpr int WPT = kTrackWarps / TW;                            // warps consuming each tile
+    static_assert(!HALF || 2 * WPT * kSub == kTile, "HALF: a warp pair's four half-warps cover a tile");
+    static_assert(kRing % TW == 0, "a ring slot holds tiles of one warp pair");
+    const int g0 = HALF ? (2 * (warp % WPT) + (lane >> 4)) * (kSub / 4) : sl * (kTile / 4 / S);
+    const int g1 = HALF ? g0 + kSub / 4 : g0 + kTile / 4 / S;
 
     float ph[PPT][3], pl[PPT][3], a[PPT][3];
 #pragma unroll
@@ -529,9 +537,10 @@ static __device__ int64_t unit_sum_f32c(const TrackParams &P, const PointSrc &sr
 
     const int64_t nt = U.t_end - U.t_beg;
     // Warps run through the ring independently: a warp waits only for its next tile to
-    // land; the last warp done with a slot refills it with the tile kRing further on.
+    // land; the last warp done with a slot refills it with the tile kRing further on (HALF:
+    // a slot holds tiles of one parity, kRing being even, and so one warp pair's).
     bool ok_all = true;
-    for (int64_t t = 0; t < nt; ++t) {
+    for (int64_t t = HALF ? warp / WPT : 0; t < nt; t += TW) {
         const uint32_t k = kt + (uint32_t)t;
         const int s = resident ? (int)t : (int)(k % kRing);
         if (!resident) {
@@ -542,9 +551,9 @@ static __device__ int64_t unit_sum_f32c(const TrackParams &P, const PointSrc &sr
             }
         }
         if (GRAD) tile_grad_f32c<PPT, kGradUnroll>(sm.ring[s], ph, pl, a, acc, g0, g1);
-        else tile_f32c<PPT, kTrackUnroll, kTrackRcp, HALF ? kSub / 8 : kSub / 4>(sm.ring[s], ph, pl, acc, g0, g1);
+        else tile_f32c<PPT, kTrackUnroll, kTrackRcp>(sm.ring[s], ph, pl, acc, g0, g1);
         if (resident) continue;
-        if (cctdev::ring_release_last(&sm.released[s], kTrackWarps) && t + kRing < nt) {
+        if (cctdev::ring_release_last(&sm.released[s], WPT) && t + kRing < nt) {
             const unsigned char *tiles = P.tiles + (P.tile_off[U.d] + U.t_beg) * (int64_t)kTileBytes;
             sm.last_issued[s] = k + kRing;
             cctdev::fence_proxy_async();
