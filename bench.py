@@ -598,12 +598,13 @@ def measure_cpu_baselines(args, ds):
     return cpu, cpu_track, acc
 
 
-def measure_reference_gpu_baseline():
+def measure_reference_gpu_baseline(steps_f32: int = 0, steps_f64: int = 0):
     """cctpy's own CUDA tracking kernel on this GPU, beside the engine on the same inputs: the
     workload of cctpy's GPU speed test (100 copies of its 24 000-segment AG-CCT beamline, 16
     copies of the ideal 250 MeV proton each, 20 mm RK4 step).  FLOAT32 (1024 threads a block,
     the speed test's configuration) over the whole 10.87 m; FLOAT64 (512 threads) over 1/32 of
-    it (0.34 m) from 4.9 m on the design orbit, into the AG-CCT.  cctpy's kernel source (final_code/packages/gpu_accelerator.py:100-1078)
+    it (0.34 m) from 4.9 m on the design orbit, into the AG-CCT.  steps_f32 / steps_f64 > 0
+    shorten the two legs to that many 20 mm steps (small cases for profiling).  cctpy's kernel source (final_code/packages/gpu_accelerator.py:100-1078)
     is compiled for sm_103a from cctpy's tree at build time (oracle/ref_cuda_build.py) and
     launched as cctpy's host code does (gpu_accelerator.py:1931-2031; oracle/ref_cuda.py);
     its per-call JIT compile is left out.  "call" times include cctpy's array packing (segment
@@ -626,12 +627,12 @@ def measure_reference_gpu_baseline():
     out = {"kernel": "cctpy track_multi_particle_beamline_for_magnet_with_multi_qs, compiled from its source "
                      "for sm_103a, one block per beamline",
            "workload": f"100 beamlines x {n_seg} segments (cctpy's GPU speed test), 16 protons each, 20 mm step"}
-    for prec, ours_prec, frac in (("f32", "f32c", 1.0), ("f64", "f64", 1.0 / 32)):
+    for prec, ours_prec, frac, n_steps in (("f32", "f32c", 1.0, steps_f32), ("f64", "f64", 1.0 / 32, steps_f64)):
         ps = particles_to_array([ParticleFactory.create_proton_along(bl, starts[prec])] * 16)
         ref = ref_cuda.ReferenceCudaTracker(prec)
         try:
             ref.track(designs[:2], ps, 0.04, 0.02)                              # module loaded, warm
-            dist = L * frac
+            dist = 0.02 * n_steps if n_steps > 0 else L * frac
             theirs, k_s, call_s = ref.track(designs, ps, dist, 0.02)
         finally:
             ref.close()
@@ -866,9 +867,19 @@ def main():
     ap.add_argument("--traffic", type=float, default=None,
                     help="DRAM bytes per launch of the timed kernel from an ncu capture (default: the committed "
                          "capture of the field-map launch)")
+    ap.add_argument("--only", choices=["speed-test"], default=None,
+                    help="speed-test: only cctpy's speed-test shape, the engine beside cctpy's own CUDA kernel "
+                         "(reference_gpu_baseline), over --speed-test-steps steps; for profiling")
+    ap.add_argument("--speed-test-steps", type=int, default=8)
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3
+    if args.only == "speed-test":
+        import torch
+        torch.cuda.set_device(0)
+        n = args.speed_test_steps
+        print(json.dumps({"only": "speed-test", "reference_gpu_baseline": measure_reference_gpu_baseline(n, n)}))
+        return
     if args.impl == "reference":
         run_reference(args)
     else:
