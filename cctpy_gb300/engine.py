@@ -546,7 +546,7 @@ def set_units_per_cta(n: int = 0) -> None:
 
 
 def set_particle_block(n: int = 0) -> None:
-    """Set the FP32c particle block by hand: 32, 64, 128 or 256 (0 restores the automatic
+    """Set the FP32c particle block by hand: 16, 32, 64, 128 or 256 (0 restores the automatic
     choice)."""
     _lib.check(_lib.load().cct_track_set_particle_block(int(n)), "cct_track_set_particle_block")
 

@@ -171,8 +171,9 @@ int cct_track_status(const void *d_scratch, void *stream);
  *  - the FP32c particle block: particles whose field sums a unit computes
  *    together (16, 32, 64, 128 or 256; 0 = automatic: 16 for designs of at most
  *    16 particles, else the power of two from 32 that needs the fewest particle
- *    slots, the largest of those).  FP64 tracking always uses blocks of 32, and
- *    cct_track_adjoint the automatic choice from 32 up.
+ *    slots, the largest of those).  FP64 tracking uses blocks of 16 for designs
+ *    of at most 16 particles and blocks of 32 otherwise, whatever the setting,
+ *    and cct_track_adjoint the automatic choice from 32 up.
  * cct_autotune times a few RK4 steps of the caller's problem (`steps` steps of
  * `footstep`, on a copy of d_particles, which is not modified) for every
  * particle block from the automatic one up to the first that holds all of a
