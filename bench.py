@@ -598,13 +598,18 @@ def measure_cpu_baselines(args, ds):
     return cpu, cpu_track, acc
 
 
-def measure_reference_gpu_baseline(steps_f32: int = 0, steps_f64: int = 0):
+def measure_reference_gpu_baseline(steps_f32: int = 0, steps_f64: int = 0, tracking=None):
     """cctpy's own CUDA tracking kernel on this GPU, beside the engine on the same inputs: the
     workload of cctpy's GPU speed test (100 copies of its 24 000-segment AG-CCT beamline, 16
     copies of the ideal 250 MeV proton each, 20 mm RK4 step).  FLOAT32 (1024 threads a block,
     the speed test's configuration) over the whole 10.87 m; FLOAT64 (512 threads) over 1/32 of
     it (0.34 m) from 4.9 m on the design orbit, into the AG-CCT.  steps_f32 / steps_f64 > 0
-    shorten the two legs to that many 20 mm steps (small cases for profiling).  cctpy's kernel source (final_code/packages/gpu_accelerator.py:100-1078)
+    shorten the two legs to that many 20 mm steps (small cases for profiling).  With
+    `tracking` (this run's tracking block) also the gantry workloads, through cctpy's FLOAT32 x
+    1024 kernel sized for 700 000 current elements a beamline: cctpy runs a design's particles
+    one after another in one block, so its rate per pair does not depend on the particle count
+    and a bounded sample (64 protons, 2 steps of 1 mm) gives it; the engine is timed on the
+    same sample and its full-configuration rate is taken from `tracking`.  cctpy's kernel source (final_code/packages/gpu_accelerator.py:100-1078)
     is compiled for sm_103a from cctpy's tree at build time (oracle/ref_cuda_build.py) and
     launched as cctpy's host code does (gpu_accelerator.py:1931-2031; oracle/ref_cuda.py);
     its per-call JIT compile is left out.  "call" times include cctpy's array packing (segment
@@ -650,6 +655,44 @@ def measure_reference_gpu_baseline(steps_f32: int = 0, steps_f64: int = 0):
                      f"ours_{ours_prec}_seconds": ours_s, "ours_gpairs_per_s": pairs / ours_s / 1e9,
                      "ours_over_reference_kernel": k_s / ours_s, "ours_over_reference_call": call_s / ours_s,
                      f"max_pos_diff_m_vs_ours_{ours_prec}": float(np.abs(theirs[:, :, :3] - mine[:, :, :3]).max())}
+    if tracking is None:
+        return out
+    from cctpy_gb300 import HUST_SC_GANTRY
+    g = W.build_gantry_section()
+    samples = {
+        "gantry_section": ([engine.host_design(engine.magnet_list(g))],
+                           W.beam_particles(g, 4096, seed=2, kinetic_MeV=215.0)[:64],
+                           tracking.get("gantry_section", {}).get("f32c", {}).get("gpairs_per_s")),
+    }
+    if "design_population" in tracking:
+        bls = [HUST_SC_GANTRY(**kw).create_second_bending_part_beamline() for kw in W.design_population(64, seed=3)]
+        samples["design_population"] = ([engine.host_design(engine.magnet_list(b)) for b in bls],
+                                        W.beam_particles(bls[0], 512, seed=2, kinetic_MeV=215.0)[:64],
+                                        tracking["design_population"].get("f32c", {}).get("gpairs_per_s"))
+    ref = ref_cuda.ReferenceCudaTracker("f32_700k")
+    try:
+        for name, (designs_g, ps_g, ours_full) in samples.items():
+            steps, step = 2, 0.001
+            ref.track(designs_g[:1], ps_g[:2], step, step)                         # warm
+            theirs, k_s, call_s = ref.track(designs_g, ps_g, steps * step, step)
+            ds_g = engine.DesignSet(designs_g)
+            engine.track(ds_g, ps_g, step, step, "f32c")
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            mine = engine.track(ds_g, ps_g, steps * step, step, "f32c")
+            torch.cuda.synchronize()
+            ours_s = time.perf_counter() - t0
+            pairs = len(ps_g) * steps * 4 * sum(d[0].shape[0] for d in designs_g)
+            rate = pairs / k_s / 1e9
+            out[name] = {"sample": f"{len(designs_g)} design(s), {sum(d[0].shape[0] for d in designs_g)} segments, "
+                                   f"{len(ps_g)} protons each, {steps} steps of 1 mm",
+                         "block": ref.block, "max_current_element_number": ref.max_ce, "kernel_seconds": k_s,
+                         "call_seconds": call_s, "gpairs_per_s": rate, "ours_f32c_same_sample_seconds": ours_s,
+                         "ours_f32c_full_configuration_gpairs_per_s": ours_full,
+                         "ours_full_configuration_over_reference_kernel": ours_full / rate if ours_full else None,
+                         "max_pos_diff_m_vs_ours_f32c": float(np.abs(theirs[:, :, :3] - mine[:, :, :3]).max())}
+    finally:
+        ref.close()
     return out
 
 
@@ -792,7 +835,7 @@ def run_ours(args):
             cpu, cpu_track, acc_oracle = measure_cpu_baselines(args, ds)
             if not (args.no_tracking or args.no_speed_test):
                 try:
-                    ref_gpu = measure_reference_gpu_baseline()
+                    ref_gpu = measure_reference_gpu_baseline(tracking=tracking)
                 except Exception as e:   # the headline line is printed whatever happens to this leg
                     ref_gpu = {"error": f"{type(e).__name__}: {e}"[:300]}
         line = {

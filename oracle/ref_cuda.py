@@ -85,8 +85,10 @@ def pack(designs, particles: np.ndarray, max_ce: int, max_qs: int, dtype) -> dic
 
 
 class ReferenceCudaTracker:
-    """cctpy's GPU tracking kernel in one precision ("f32": FLOAT32 x 1024 threads, "f64":
-    FLOAT64 x 512 threads), loaded on the current CUDA device."""
+    """cctpy's GPU tracking kernel in one of the built configurations ("f32": FLOAT32 x 1024
+    threads, "f64": FLOAT64 x 512 threads, both with cctpy's default capacities; "f32_700k":
+    FLOAT32 x 1024 with room for 700 000 current elements a beamline), loaded on the current
+    CUDA device."""
 
     def __init__(self, precision: str = "f32"):
         import torch
@@ -99,8 +101,9 @@ class ReferenceCudaTracker:
         self.block = int(cfg["block"])
         self.max_ce = int(cfg["max_current_element_number"])
         self.max_qs = int(cfg["max_qs_datas_length"])
-        self.np_dtype = np.float32 if precision == "f32" else np.float64
-        self.torch_dtype = torch.float32 if precision == "f32" else torch.float64
+        single = int(cfg["float_bytes"]) == 4
+        self.np_dtype = np.float32 if single else np.float64
+        self.torch_dtype = torch.float32 if single else torch.float64
         torch.zeros(1, device="cuda")                    # torch's primary context is current
         self.drv = _Driver()
         self.module = ctypes.c_void_p()

@@ -10,7 +10,12 @@ gpu_accelerator.py:54-70), wraps it in ``extern "C"`` as pycuda does, and compil
 nvcc into device-only cubins:
 
     oracle/_ref/cctpy_track_f32.cubin, oracle/_ref/cctpy_track_f64.cubin,
+    oracle/_ref/cctpy_track_f32_700k.cubin,
     oracle/_ref/cctpy_cuda.json (block sizes, array capacities, registers, source hash)
+
+The third is FLOAT32 x 1024 with room for 700 000 current elements a beamline (the
+``max_current_element_number`` constructor argument): the gantry-section and population
+designs (up to ~625 000 segments) exceed cctpy's default of 240 000.
 
 The source is written to a temporary directory outside the repository and deleted after the
 compile; only the device binaries and their description are kept (``oracle/_ref/`` is
@@ -33,9 +38,10 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_ref")
 META = os.path.join(OUT, "cctpy_cuda.json")
 KERNEL = "track_multi_particle_beamline_for_magnet_with_multi_qs"
-# (name, cctpy float type, block_dim_x): the speed test's FLOAT32 x 1024 and the FLOAT64
-# block size cctpy's docstring asks for (1024 may exceed the register file in FP64)
-CONFIGS = (("f32", "FLOAT32", 1024), ("f64", "FLOAT64", 512))
+# (name, cctpy float type, block_dim_x, max_current_element_number or None for cctpy's
+# default): the speed test's FLOAT32 x 1024, the FLOAT64 block size cctpy's docstring asks for
+# (1024 may exceed the register file in FP64), and FLOAT32 x 1024 sized for gantry designs
+CONFIGS = (("f32", "FLOAT32", 1024, None), ("f64", "FLOAT64", 512, None), ("f32_700k", "FLOAT32", 1024, 700_000))
 
 
 def _stub_plotting():
@@ -61,8 +67,10 @@ def cuda_sources(ref_dir: str) -> dict:
     sys.path.insert(0, os.path.join(ref_dir, "final_code"))
     from packages.gpu_accelerator import GPU_ACCELERATOR
     out = {}
-    for name, ftype, block in CONFIGS:
-        ga = GPU_ACCELERATOR(float_number_type=getattr(GPU_ACCELERATOR, ftype), block_dim_x=block, cpu_mode=True)
+    for name, ftype, block, max_ce in CONFIGS:
+        kw = {} if max_ce is None else {"max_current_element_number": max_ce}
+        ga = GPU_ACCELERATOR(float_number_type=getattr(GPU_ACCELERATOR, ftype), block_dim_x=block, cpu_mode=True,
+                             **kw)
         out[name] = (ga.cuda_code, ga.block_dim_x, ga.max_current_element_number, ga.max_qs_datas_length)
     return out
 
@@ -85,7 +93,9 @@ def build(ref_dir: str, nvcc: str = "nvcc", force: bool = False) -> dict:
     meta = {"kernel": KERNEL, "source": "final_code/packages/gpu_accelerator.py", "source_sha256": sha,
             "arch": "sm_103a", "configs": {}}
     with tempfile.TemporaryDirectory() as tmp:
+        ftypes = {c[0]: c[1] for c in CONFIGS}
         for name, (code, block, max_ce, max_qs) in cuda_sources(ref_dir).items():
+            ftype = ftypes[name]
             cu = os.path.join(tmp, f"cctpy_{name}.cu")
             with open(cu, "w") as f:      # pycuda's SourceModule wraps the source the same way
                 f.write('extern "C" {\n' + code + "\n}\n")
@@ -107,7 +117,7 @@ def build(ref_dir: str, nvcc: str = "nvcc", force: bool = False) -> dict:
                 raise RuntimeError(f"cctpy's {name} kernel uses {regs} registers: {block} threads do not fit an SM")
             meta["configs"][name] = {"cubin": os.path.basename(cubin), "block": block,
                                      "max_current_element_number": max_ce, "max_qs_datas_length": max_qs,
-                                     "registers": regs, "float_bytes": 4 if name == "f32" else 8}
+                                     "registers": regs, "float_bytes": 8 if ftype == "FLOAT64" else 4}
     with open(META, "w") as f:
         json.dump(meta, f, indent=1)
     return meta

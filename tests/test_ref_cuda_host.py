@@ -15,17 +15,17 @@ import __graft_entry__ as G
 from oracle import ref_cuda, ref_cuda_build
 
 
-def test_recipe_builds_both_configurations():
+def test_recipe_builds_every_configuration():
     if not os.path.isdir(os.path.join(G.REFERENCE_TREE, "final_code")):
         pytest.skip("cctpy's sources are not on this machine")
     meta = ref_cuda_build.build(G.REFERENCE_TREE)
     assert meta["kernel"] == "track_multi_particle_beamline_for_magnet_with_multi_qs"
-    assert set(meta["configs"]) == {"f32", "f64"}
-    for name, block, width in (("f32", 1024, 4), ("f64", 512, 8)):
+    assert set(meta["configs"]) == {"f32", "f64", "f32_700k"}
+    for name, block, width, cap in (("f32", 1024, 4, 240000), ("f64", 512, 8, 240000), ("f32_700k", 1024, 4, 700000)):
         c = meta["configs"][name]
         assert c["block"] == block and c["float_bytes"] == width
         assert c["registers"] is not None and c["registers"] * block <= 65536
-        assert c["max_current_element_number"] == 240000 and c["max_qs_datas_length"] == 10000
+        assert c["max_current_element_number"] == cap and c["max_qs_datas_length"] == 10000
         assert os.path.getsize(os.path.join(ref_cuda.REF_DIR, c["cubin"])) > 0
     assert not [f for f in os.listdir(ref_cuda.REF_DIR) if f.endswith((".cu", ".cuh", ".py", ".c"))]
     assert ref_cuda.available()
