@@ -12,8 +12,10 @@ conventions and errors:
 Differences, by design of this engine:
 
 * FLOAT32 selects the FP32-compensated kernels (<= 1e-7 relative field error),
-  FLOAT64 the plain FP64 kernels; nothing is JIT-compiled per call and segment sets
-  stay resident in HBM between calls;
+  FLOAT64 the plain FP64 kernels; nothing is JIT-compiled per call; a beamline object
+  given several times in one call has its segments built and copied to the device once
+  (every call still builds them afresh, as the reference does, so that changes to the
+  magnets between calls are seen; ``cctpy_gb300.engine`` keeps design sets resident);
 * every design of a population runs in one persistent launch (no block-per-design
   serial particle loop), so ``block_dim_x`` only keeps its validation;
 * segment counts are not padded to ``max_current_element_number``; exceeding it still
@@ -132,7 +134,11 @@ class GPU_ACCELERATOR:
     def _multi_beamline(self, bls, ps, distance, footstep, single_qs):
         if not bls:
             return []
-        out = self._track([self._design(engine.magnet_list(b), single_qs) for b in bls], ps, distance, footstep)
+        built = {}
+        for b in bls:      # the same beamline object several times: one design, repeated on the device
+            if id(b) not in built:
+                built[id(b)] = self._design(engine.magnet_list(b), single_qs)
+        out = self._track([built[id(b)] for b in bls], ps, distance, footstep)
         return [[RunningParticle.from_numpy_array_data(r) for r in row] for row in out]
 
     def track_multi_particle_beamline_for_magnet_with_single_qs(self, bls: list, ps: List[RunningParticle],

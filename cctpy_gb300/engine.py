@@ -236,10 +236,21 @@ class DesignSet:
 
     def __init__(self, designs: Sequence[tuple]):
         seg_counts = [d[0].shape[0] for d in designs]
-        cat = lambda k, w: np.concatenate([d[k] for d in designs]) if designs else np.zeros((0, w))
+        # a design given several times (the same tuple object) is copied to the device once
+        # and repeated there
+        first = {}
+        order = [first.setdefault(id(d), len(first)) for d in designs]
+        uniq = [None] * len(first)
+        for d, i in zip(designs, order):
+            uniq[i] = d
+        cat = lambda k, w: np.concatenate([d[k] for d in uniq]) if uniq else np.zeros((0, w))
         dev = _device()
-        self._finish(seg_counts, [d[2] for d in designs], torch.from_numpy(cat(0, 3)).to(dev),
-                     torch.from_numpy(cat(1, 3)).to(dev))
+        kls, p0s = torch.from_numpy(cat(0, 3)).to(dev), torch.from_numpy(cat(1, 3)).to(dev)
+        if len(uniq) < len(designs):
+            off = np.concatenate([[0], np.cumsum([d[0].shape[0] for d in uniq])]).astype(np.int64)
+            kls = torch.cat([kls[off[i]:off[i + 1]] for i in order])
+            p0s = torch.cat([p0s[off[i]:off[i + 1]] for i in order])
+        self._finish(seg_counts, [d[2] for d in designs], kls, p0s)
 
     def _finish(self, seg_counts, qs_list, kls, p0s):
         dev = kls.device
@@ -358,7 +369,11 @@ def design_set_of(objs: Sequence, segments: str = "host") -> DesignSet:
     """Design set of several beamlines / magnets.  segments="host" builds the segment arrays
     with numpy and copies them; "device" generates them on the GPU from layer records."""
     if segments == "host":
-        return DesignSet([host_design(magnet_list(o)) for o in objs])
+        built = {}
+        for o in objs:      # an object given several times: built once, repeated on the device
+            if id(o) not in built:
+                built[id(o)] = host_design(magnet_list(o))
+        return DesignSet([built[id(o)] for o in objs])
     if segments != "device":
         raise ValueError(f"segments must be 'host' or 'device', not {segments!r}")
     parts = [device_layers(magnet_list(o)) for o in objs]

@@ -117,6 +117,20 @@ def test_accelerator_conventions(golden):
     many = [p.copy() for p in ps]
     ParticleRunner.run_only(many, bl, L, 0.1)
     check(particles_to_array(many), golden["h2_particles_out"], POS_TOL_F64, VEL_RTOL_F64)
+    # the same beamline object given several times is built once and repeated on the device:
+    # the results equal, bit for bit, those of a call of the same shape with a separately
+    # built copy (calls of different shapes split the segment sums differently)
+    bl2 = HUST_SC_GANTRY().create_second_bending_part_beamline()
+    mixed = ga.track_multi_particle_beamline_for_magnet_with_multi_qs([bl, bl2, bl], ps, L, 0.1)
+    same = ga.track_multi_particle_beamline_for_magnet_with_multi_qs([bl, bl, bl], ps, L, 0.1)
+    for a, b in zip(mixed, same):
+        np.testing.assert_array_equal(particles_to_array(a), particles_to_array(b))
+        check(particles_to_array(a), golden["h2_particles_out"], POS_TOL_F64, VEL_RTOL_F64)
+    d = engine.host_design(engine.magnet_list(bl))
+    rep = engine.DesignSet([d, d, d])
+    sep = engine.DesignSet([d, tuple(np.copy(a) for a in d), d])
+    assert torch.equal(rep.kls, sep.kls) and torch.equal(rep.p0s, sep.p0s) and torch.equal(rep.qs, sep.qs)
+    assert np.array_equal(rep.h_seg_off, sep.h_seg_off)
     with pytest.raises(ValueError):
         GPU_ACCELERATOR(block_dim_x=1000)
     with pytest.raises(ValueError):
