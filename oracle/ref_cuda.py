@@ -86,9 +86,9 @@ def pack(designs, particles: np.ndarray, max_ce: int, max_qs: int, dtype) -> dic
 
 class ReferenceCudaTracker:
     """cctpy's GPU tracking kernel in one of the built configurations ("f32": FLOAT32 x 1024
-    threads, "f64": FLOAT64 x 512 threads, both with cctpy's default capacities; "f32_700k":
-    FLOAT32 x 1024 with room for 700 000 current elements a beamline), loaded on the current
-    CUDA device."""
+    threads, "f64": FLOAT64 x 512 threads, both with cctpy's default capacities; "f32_700k",
+    "f64_700k": the same with room for 700 000 current elements a beamline), loaded on the
+    current CUDA device."""
 
     def __init__(self, precision: str = "f32"):
         import torch

@@ -10,10 +10,10 @@ gpu_accelerator.py:54-70), wraps it in ``extern "C"`` as pycuda does, and compil
 nvcc into device-only cubins:
 
     oracle/_ref/cctpy_track_f32.cubin, oracle/_ref/cctpy_track_f64.cubin,
-    oracle/_ref/cctpy_track_f32_700k.cubin,
+    oracle/_ref/cctpy_track_f32_700k.cubin, oracle/_ref/cctpy_track_f64_700k.cubin,
     oracle/_ref/cctpy_cuda.json (block sizes, array capacities, registers, source hash)
 
-The third is FLOAT32 x 1024 with room for 700 000 current elements a beamline (the
+The last two have room for 700 000 current elements a beamline (the
 ``max_current_element_number`` constructor argument): the gantry-section and population
 designs (up to ~625 000 segments) exceed cctpy's default of 240 000.
 
@@ -40,8 +40,9 @@ META = os.path.join(OUT, "cctpy_cuda.json")
 KERNEL = "track_multi_particle_beamline_for_magnet_with_multi_qs"
 # (name, cctpy float type, block_dim_x, max_current_element_number or None for cctpy's
 # default): the speed test's FLOAT32 x 1024, the FLOAT64 block size cctpy's docstring asks for
-# (1024 may exceed the register file in FP64), and FLOAT32 x 1024 sized for gantry designs
-CONFIGS = (("f32", "FLOAT32", 1024, None), ("f64", "FLOAT64", 512, None), ("f32_700k", "FLOAT32", 1024, 700_000))
+# (1024 may exceed the register file in FP64), and both sized for gantry designs
+CONFIGS = (("f32", "FLOAT32", 1024, None), ("f64", "FLOAT64", 512, None), ("f32_700k", "FLOAT32", 1024, 700_000),
+           ("f64_700k", "FLOAT64", 512, 700_000))
 
 
 def _stub_plotting():

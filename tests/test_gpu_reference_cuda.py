@@ -72,3 +72,39 @@ def test_fp32c_closer_to_fp64_than_cctpy_fp32_kernel():
     assert err_ours * 10 < err_ref, f"FP32c {err_ours:.3e} m against cctpy's FLOAT32 kernel {err_ref:.3e} m"
     # the reference's FP32 kernel still tracks the same beam (its documented error: ~0.05 mm)
     assert err_ref < 1e-3
+
+
+def test_gantry_designs_match_cctpy_cuda_kernel():
+    """The workloads' own magnets through cctpy's kernels built with room for 700 000 current
+    elements a beamline: the gantry section (597 600 segments + QS) and two designs of the
+    population (their own, ragged segment counts: each block of cctpy's kernel reads its own
+    padded slice), four 215 MeV protons each, 10 RK4 steps of the workloads' 1 mm from the
+    start of the section.  FP64 agrees with cctpy's FLOAT64 kernel to rounding; FP32c is far
+    closer to FP64 than cctpy's FLOAT32 kernel, which keeps positions in FP32."""
+    ref_cuda, engine, _, _ = _setup()
+    from cctpy_gb300 import HUST_SC_GANTRY, workloads as W
+    g = W.build_gantry_section()
+    pop = [HUST_SC_GANTRY(**kw).create_second_bending_part_beamline() for kw in W.design_population(2, seed=3)]
+    designs = [engine.host_design(engine.magnet_list(b)) for b in [g] + pop]
+    assert designs[0][0].shape[0] == 597600 and len({d[0].shape[0] for d in designs}) == 3
+    ps = W.beam_particles(g, N_P, seed=2, kinetic_MeV=215.0)
+    L, step = 0.01, 0.001
+    ds = engine.DesignSet(designs)
+    truth = engine.track(ds, ps, L, step, "f64")
+    ours = engine.track(ds, ps, L, step, "f32c")
+    got = {}
+    for cfg in ("f64_700k", "f32_700k"):
+        ref = ref_cuda.ReferenceCudaTracker(cfg)
+        try:
+            got[cfg] = ref.track(designs, ps, L, step)[0]
+        finally:
+            ref.close()
+    want = got["f64_700k"]
+    pos = np.abs(truth[:, :, :3] - want[:, :, :3]).max()
+    vel = (np.abs(truth[:, :, 3:6] - want[:, :, 3:6]) / np.abs(want[:, :, 3:6]).max()).max()
+    assert pos < 1e-12, f"FP64 positions differ from cctpy's CUDA kernel by {pos:.3e} m"
+    assert vel < 1e-12, f"FP64 velocities differ from cctpy's CUDA kernel by {vel:.3e} (relative)"
+    err_ours = np.abs(ours[:, :, :3] - truth[:, :, :3]).max()
+    err_ref = np.abs(got["f32_700k"][:, :, :3] - truth[:, :, :3]).max()
+    assert err_ours < 1e-8, f"FP32c position error {err_ours:.3e} m"
+    assert err_ours * 10 < err_ref, f"FP32c {err_ours:.3e} m against cctpy's FLOAT32 kernel {err_ref:.3e} m"

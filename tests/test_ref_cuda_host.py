@@ -20,8 +20,9 @@ def test_recipe_builds_every_configuration():
         pytest.skip("cctpy's sources are not on this machine")
     meta = ref_cuda_build.build(G.REFERENCE_TREE)
     assert meta["kernel"] == "track_multi_particle_beamline_for_magnet_with_multi_qs"
-    assert set(meta["configs"]) == {"f32", "f64", "f32_700k"}
-    for name, block, width, cap in (("f32", 1024, 4, 240000), ("f64", 512, 8, 240000), ("f32_700k", 1024, 4, 700000)):
+    assert set(meta["configs"]) == {"f32", "f64", "f32_700k", "f64_700k"}
+    for name, block, width, cap in (("f32", 1024, 4, 240000), ("f64", 512, 8, 240000), ("f32_700k", 1024, 4, 700000),
+                                    ("f64_700k", 512, 8, 700000)):
         c = meta["configs"][name]
         assert c["block"] == block and c["float_bytes"] == width
         assert c["registers"] is not None and c["registers"] * block <= 65536
