@@ -687,6 +687,8 @@ def measure_reference_gpu_baseline(steps_f32: int = 0, steps_f64: int = 0, track
             steps, step = 2, 0.001
             ref.track(designs_g[:1], ps_g[:2], step, step)                         # warm
             theirs, k_s, call_s = ref.track(designs_g, ps_g, steps * step, step)
+            half = len(ps_g) // 2     # half the protons: cctpy's per-pair rate should not change
+            _, k_half, _ = ref.track(designs_g, ps_g[:half], steps * step, step)
             ds_g = engine.DesignSet(designs_g)
             engine.track(ds_g, ps_g, step, step, "f32c")
             torch.cuda.synchronize()
@@ -699,7 +701,9 @@ def measure_reference_gpu_baseline(steps_f32: int = 0, steps_f64: int = 0, track
             out[name] = {"sample": f"{len(designs_g)} design(s), {sum(d[0].shape[0] for d in designs_g)} segments, "
                                    f"{len(ps_g)} protons each, {steps} steps of 1 mm",
                          "block": ref.block, "max_current_element_number": ref.max_ce, "kernel_seconds": k_s,
-                         "call_seconds": call_s, "gpairs_per_s": rate, "ours_f32c_same_sample_seconds": ours_s,
+                         "call_seconds": call_s, "gpairs_per_s": rate,
+                         f"gpairs_per_s_with_{half}_protons": pairs * half / len(ps_g) / k_half / 1e9,
+                         "ours_f32c_same_sample_seconds": ours_s,
                          "ours_f32c_full_configuration_gpairs_per_s": ours_full,
                          "ours_full_configuration_over_reference_kernel": ours_full / rate if ours_full else None,
                          "max_pos_diff_m_vs_ours_f32c": float(np.abs(theirs[:, :, :3] - mine[:, :, :3]).max())}
