@@ -23,7 +23,13 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 REF_DIR = os.path.join(HERE, "_ref")
 META = os.path.join(REF_DIR, "cctpy_cuda.json")
-N_PARAMS = 9
+# cctpy's two multi-beamline kernels (gpu_accelerator.py:1023-1063) and their arguments
+KERNELS = {
+    "multi_qs": ("track_multi_particle_beamline_for_magnet_with_multi_qs",
+                 ("distance", "footstep", "kls", "p0s", "n_ce", "qs", "n_qs", "particles", "n_p")),
+    "single_qs": ("track_multi_particle_beamline_for_magnet_with_single_qs",
+                  ("distance", "footstep", "kls", "p0s", "n_ce", "qs", "particles", "n_p")),
+}
 
 
 def available() -> bool:
@@ -52,10 +58,13 @@ class _Driver:
             raise RuntimeError(f"{what} failed: {name.value.decode() if name.value else rc}")
 
 
-def pack(designs, particles: np.ndarray, max_ce: int, max_qs: int, dtype) -> dict:
+def pack(designs, particles: np.ndarray, max_ce: int, max_qs: int, dtype, single_qs: bool = False) -> dict:
     """Host arrays in cctpy's GPU layout (gpu_accelerator.py:1953-2016).  ``designs``: per
     beamline (kls (n, 3), p0s (n, 3), qs (k, 16)); ``particles``: (n_p, 10) records, given to
-    every beamline; ``max_ce`` / ``max_qs``: the kernel's compiled capacities."""
+    every beamline; ``max_ce`` / ``max_qs``: the kernel's compiled capacities.  single_qs:
+    the layout of cctpy's single-QS kernel (gpu_accelerator.py:1834-1874): one 16-number
+    record per beamline, the beamline's last QS (cctpy's host loop keeps overwriting it), and
+    a beamline without a QS refused (cctpy's concatenation of its None fails there)."""
     D = len(designs)
     parts = np.ascontiguousarray(particles, dtype=np.float64).reshape(-1, 10)
     n_p = parts.shape[0]
@@ -80,6 +89,10 @@ def pack(designs, particles: np.ndarray, max_ce: int, max_qs: int, dtype) -> dic
         qs[d, :q.size] = q
         n_ce[d] = k.size // 3
         n_qs[d] = q.size // 16
+    if single_qs:
+        if not n_qs.all():
+            raise ValueError("cctpy's single-QS kernel needs a QS in every beamline")
+        qs = np.stack([qs[d, 16 * (n_qs[d] - 1):16 * n_qs[d]] for d in range(D)])
     return dict(kls=kls, p0s=p0s, n_ce=n_ce, qs=qs, n_qs=n_qs,
                 particles=np.tile(parts, (D, 1)).astype(dtype), n_p=np.array([n_p], np.int32))
 
@@ -88,9 +101,10 @@ class ReferenceCudaTracker:
     """cctpy's GPU tracking kernel in one of the built configurations ("f32": FLOAT32 x 1024
     threads, "f64": FLOAT64 x 512 threads, both with cctpy's default capacities; "f32_700k",
     "f64_700k": the same with room for 700 000 current elements a beamline), loaded on the
-    current CUDA device."""
+    current CUDA device.  kernel: "multi_qs" (every QS of a beamline, the kernel cctpy's
+    track_multi_particle_beamline_for_magnet_with_multi_qs launches) or "single_qs"."""
 
-    def __init__(self, precision: str = "f32"):
+    def __init__(self, precision: str = "f32", kernel: str = "multi_qs"):
         import torch
         if not available():
             raise FileNotFoundError("cctpy's CUDA kernels are not built (oracle/ref_cuda_build.py)")
@@ -109,9 +123,11 @@ class ReferenceCudaTracker:
         self.module = ctypes.c_void_p()
         self.drv.check(self.drv.lib.cuModuleLoad(ctypes.byref(self.module),
                                                  os.path.join(REF_DIR, cfg["cubin"]).encode()), "cuModuleLoad")
+        self.single_qs = kernel == "single_qs"
+        name, self.args = KERNELS[kernel]
         self.fn = ctypes.c_void_p()
-        self.drv.check(self.drv.lib.cuModuleGetFunction(ctypes.byref(self.fn), self.module,
-                                                        meta["kernel"].encode()), "cuModuleGetFunction")
+        self.drv.check(self.drv.lib.cuModuleGetFunction(ctypes.byref(self.fn), self.module, name.encode()),
+                       "cuModuleGetFunction")
 
     def close(self) -> None:
         if self.module:
@@ -119,7 +135,7 @@ class ReferenceCudaTracker:
             self.module = ctypes.c_void_p()
 
     def pack(self, designs, particles: np.ndarray) -> dict:
-        return pack(designs, particles, self.max_ce, self.max_qs, self.np_dtype)
+        return pack(designs, particles, self.max_ce, self.max_qs, self.np_dtype, self.single_qs)
 
     def upload(self, host: dict, distance: float, footstep: float) -> dict:
         import torch
@@ -131,9 +147,8 @@ class ReferenceCudaTracker:
     def launch(self, dev: dict) -> None:
         """One launch on torch's current stream: grid = beamlines, block = block_dim_x."""
         import torch
-        order = ("distance", "footstep", "kls", "p0s", "n_ce", "qs", "n_qs", "particles", "n_p")
-        ptrs = [ctypes.c_void_p(dev[k].data_ptr()) for k in order]
-        params = (ctypes.c_void_p * N_PARAMS)(*[ctypes.cast(ctypes.pointer(p), ctypes.c_void_p) for p in ptrs])
+        ptrs = [ctypes.c_void_p(dev[k].data_ptr()) for k in self.args]
+        params = (ctypes.c_void_p * len(ptrs))(*[ctypes.cast(ctypes.pointer(p), ctypes.c_void_p) for p in ptrs])
         stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
         D = int(dev["n_ce"].shape[0])
         self.drv.check(self.drv.lib.cuLaunchKernel(self.fn, D, 1, 1, self.block, 1, 1, 0, stream, params, None),

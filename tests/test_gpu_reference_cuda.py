@@ -108,3 +108,33 @@ def test_gantry_designs_match_cctpy_cuda_kernel():
     err_ref = np.abs(got["f32_700k"][:, :, :3] - truth[:, :, :3]).max()
     assert err_ours < 1e-8, f"FP32c position error {err_ours:.3e} m"
     assert err_ours * 10 < err_ref, f"FP32c {err_ours:.3e} m against cctpy's FLOAT32 kernel {err_ref:.3e} m"
+
+
+def test_single_qs_calls_match_cctpy_single_qs_kernel():
+    """cctpy's single-QS beamline kernel (track_multi_particle_beamline_for_magnet_with_single_qs,
+    gpu_accelerator.py:1023-1041) gets one QS a beamline, the last one its host loop sees
+    (gpu_accelerator.py:1834-1874).  The gantry's first bending section has three: the drop-in
+    accelerator's single-QS call must agree with cctpy's kernel to rounding in FP64, and differ
+    from the multi-QS call (which sums all three) by far more."""
+    ref_cuda, engine, _, _ = _setup()
+    from cctpy_gb300 import GPU_ACCELERATOR, HUST_SC_GANTRY, RunningParticle, workloads as W
+    from cctpy_gb300.particles import particles_to_array
+    bl = HUST_SC_GANTRY().create_first_bending_part_beamline()
+    design = engine.host_design(engine.magnet_list(bl))
+    assert design[2].shape[0] == 3
+    ps = W.beam_particles(bl, N_P, seed=3, kinetic_MeV=215.0)
+    L, step = bl.get_length(), 0.05
+    ref = ref_cuda.ReferenceCudaTracker("f64", kernel="single_qs")
+    try:
+        want = ref.track([design, design], ps, L, step)[0]
+    finally:
+        ref.close()
+    ga = GPU_ACCELERATOR(GPU_ACCELERATOR.FLOAT64, block_dim_x=512)
+    rps = [RunningParticle.from_numpy_array_data(r) for r in ps]
+    single = np.stack([particles_to_array(row) for row in
+                       ga.track_multi_particle_beamline_for_magnet_with_single_qs([bl, bl], rps, L, step)])
+    multi = np.stack([particles_to_array(row) for row in
+                      ga.track_multi_particle_beamline_for_magnet_with_multi_qs([bl, bl], rps, L, step)])
+    pos = np.abs(single[:, :, :3] - want[:, :, :3]).max()
+    assert pos < 1e-12, f"single-QS FP64 positions differ from cctpy's single-QS kernel by {pos:.3e} m"
+    assert np.abs(multi[:, :, :3] - want[:, :, :3]).max() > 1e-6

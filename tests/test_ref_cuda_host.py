@@ -68,3 +68,20 @@ def test_packing_refuses_what_the_kernel_cannot_hold():
         ref_cuda.pack([seg(2)], np.zeros((0, 10)), 8, 2, np.float64)
     with pytest.raises(ValueError):
         ref_cuda.pack([(np.zeros((2, 3)), np.zeros((3, 3)), np.zeros((0, 16)))], parts, 8, 2, np.float64)
+
+
+def test_single_qs_packing_keeps_each_beamlines_last_qs():
+    rng = np.random.default_rng(2)
+    parts = rng.normal(size=(3, 10))
+    q3, q1 = rng.normal(size=(3, 16)), rng.normal(size=(1, 16))
+    designs = [(rng.normal(size=(4, 3)), rng.normal(size=(4, 3)), q3),
+               (rng.normal(size=(2, 3)), rng.normal(size=(2, 3)), q1)]
+    h = ref_cuda.pack(designs, parts, 8, 4, np.float64, single_qs=True)
+    assert h["qs"].shape == (2, 16)
+    np.testing.assert_array_equal(h["qs"][0], q3[2])
+    np.testing.assert_array_equal(h["qs"][1], q1[0])
+    np.testing.assert_array_equal(h["kls"][0, :12], designs[0][0].reshape(-1))
+    with pytest.raises(ValueError, match="single-QS"):
+        ref_cuda.pack([(designs[0][0], designs[0][1], np.zeros((0, 16)))], parts, 8, 4, np.float64, single_qs=True)
+    assert set(ref_cuda.KERNELS) == {"multi_qs", "single_qs"}
+    assert len(ref_cuda.KERNELS["single_qs"][1]) == 8 and len(ref_cuda.KERNELS["multi_qs"][1]) == 9
