@@ -615,7 +615,9 @@ def measure_reference_gpu_baseline(steps_f32: int = 0, steps_f64: int = 0, track
     workload of cctpy's GPU speed test (100 copies of its 24 000-segment AG-CCT beamline, 16
     copies of the ideal 250 MeV proton each, 20 mm RK4 step).  FLOAT32 (1024 threads a block,
     the speed test's configuration) over the whole 10.87 m; FLOAT64 (512 threads) over 1/32 of
-    it (0.34 m) from 4.9 m on the design orbit, into the AG-CCT.  steps_f32 / steps_f64 > 0
+    it (0.34 m) from 4.9 m on the design orbit, into the AG-CCT.  With `tracking`, also C0 (the
+    single dipole's 32 protons: FLOAT32 over the whole arc, FLOAT64 over 8 steps, cctpy's
+    default build).  steps_f32 / steps_f64 > 0
     shorten the two legs to that many 20 mm steps (small cases for profiling).  With
     `tracking` (this run's tracking block) also the gantry workloads, through cctpy's FLOAT32 x
     1024 kernel sized for 700 000 current elements a beamline: cctpy runs a design's particles
@@ -669,6 +671,34 @@ def measure_reference_gpu_baseline(steps_f32: int = 0, steps_f64: int = 0, track
                      f"max_pos_diff_m_vs_ours_{ours_prec}": float(np.abs(theirs[:, :, :3] - mine[:, :, :3]).max())}
     if tracking is None:
         return out
+    # C0: the single dipole's 32 protons through cctpy's kernel (one beamline: one block),
+    # FLOAT32 over the whole arc, FLOAT64 over its first 8 steps
+    _, cct = W.build_single_dipole()
+    d0 = engine.host_design(engine.magnet_list(cct))
+    p32 = W.single_dipole_particles(32, seed=0)
+    L0 = W.single_dipole_track_length()
+    ds0 = engine.design_of(cct)
+    c0 = {"workload": f"C0: {d0[0].shape[0]} segments, 32 protons of 250 MeV, 1 mm steps"}
+    for cfg, ours_prec, steps0 in (("f32", "f32c", 0), ("f64", "f64", 8)):
+        dist = L0 if steps0 == 0 else steps0 * 0.001
+        ref = ref_cuda.ReferenceCudaTracker(cfg)
+        try:
+            ref.track([d0], p32[:2], 0.002, 0.001)                               # warm
+            theirs, k_s, call_s = ref.track([d0], p32, dist, 0.001)
+        finally:
+            ref.close()
+        engine.track(ds0, p32, 0.002, 0.001, ours_prec)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        mine = engine.track(ds0, p32, dist, 0.001, ours_prec)
+        torch.cuda.synchronize()
+        ours_s = time.perf_counter() - t0
+        steps = int(np.ceil(dist / 0.001 - 1e-9))
+        pairs = 32 * steps * 4 * d0[0].shape[0]
+        c0[cfg] = {"steps": steps, "kernel_seconds": k_s, "call_seconds": call_s, "gpairs_per_s": pairs / k_s / 1e9,
+                   f"ours_{ours_prec}_seconds": ours_s, "ours_over_reference_kernel": k_s / ours_s,
+                   f"max_pos_diff_m_vs_ours_{ours_prec}": float(np.abs(theirs[:, :, :3] - mine[:, :, :3]).max())}
+    out["single_dipole"] = c0
     from cctpy_gb300 import HUST_SC_GANTRY
     g = W.build_gantry_section()
     samples = {
